@@ -1,0 +1,315 @@
+"""Benchmark: SAD fit of a 1024x1024 image at 1.0 bpp with the full training_config.json
+schedule (128,000 sites pruned to 8,192 over 4,000 iterations), on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one whole fit of the workload.  `value` is the training-loop throughput in
+iterations/s with the image already resident in HBM (init excluded, as in the
+reference's own it/s log line); `e2e` is the same metric through the host-memory entry
+point sad_trainer_fit_host (image upload, init, all iterations, PSNR, download of the
+active sites).  L2 is flushed (512 MB write) between steps.  Under torchrun each rank
+fits its own image (replicas; no data-path collective); the barrier and the max over
+ranks only bracket the timing.
+
+--impl reference times the CPU restatement of the reference's path (the reference has
+no CPU path of its own) on all host cores, on bounded samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WIDTH = HEIGHT = 1024
+METRIC = "train iters/s @1024x1024, 1.0 bpp (training_config.json schedule)"
+WORKLOAD = ("fit of a 1024x1024 RGB f32 image at 1.0 bpp: 128000 sites pruned to 8192 "
+            "(bpp rule), 4000 iterations, VPT every 8, 73 prune events, K=8 candidates")
+DATA = "synthetic: seeded smooth gradient + 256 Gaussian blobs + 64 convex polygons, 1024x1024"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks and throttle reasons)."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        if not getattr(self, "lines", None):
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the fused gradient kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "fused_gradients_1024.json")) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def flush_l2(buf):
+    buf.fill_(1)
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import sad_gb300
+    from sad_gb300 import _lib
+    from sad_gb300.synthetic import synthetic_image
+    from sad_gb300.trainer import Trainer
+
+    lib = _lib.load()
+    img = synthetic_image(WIDTH, HEIGHT, seed=rank)
+    target = torch.from_numpy(img).cuda()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    tr = Trainer(WIDTH, HEIGHT, log_freq=0, use_graphs=1)
+    iters = tr.cfg.iterations
+    stream = torch.cuda.ExternalStream(lib.sad_trainer_stream(tr._h))
+    tr.set_target(target)
+
+    def one_fit(timed: bool):
+        tr.init()
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        tr.run()
+        ev1.record(stream)
+        ev1.synchronize()
+        return ev0.elapsed_time(ev1)
+
+    for _ in range(args.warmup):
+        one_fit(False)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.sad_launch_count()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            times.append(one_fit(True))
+    torch.cuda.synchronize()
+    launches = lib.sad_launch_count() - launches0
+    total_ms = float(sum(times))
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    psnr = tr.psnr()
+    final_sites = tr.info().active_estimate
+    value = ws * args.steps * iters / (total_ms / 1e3)
+
+    # roofline: one instrumented fit times every fused-gradient launch with CUDA events on
+    # the trainer's stream (eager launches; the kernels are the same)
+    tr.enable_timing(True)
+    tr.init()
+    tr.run()
+    info = tr.info()
+    tr.enable_timing(False)
+    grad_ms = info.gpu_ms_gradients / max(1, info.gradient_launches)
+    n_buf = info.site_buffer
+    alg_bytes = 48 * WIDTH * HEIGHT + 80 * n_buf
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (grad_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(),
+                "kernel": "fused_gradients_kernel", "launch_ms": round(grad_ms, 5),
+                "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
+
+    # e2e: host image in pinned memory -> fit -> active sites + PSNR back
+    host = torch.from_numpy(img).pin_memory().numpy()
+    e2e_t = []
+    sites_out = np.empty((tr.cfg.n_sites, 10), dtype=np.float32)
+    for i in range(max(1, args.steps)):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sites, e2e_psnr = tr.fit_host(host, sites_out)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_value = ws * len(e2e_t) * iters / sum(e2e_t)
+    e2e = {"value": round(e2e_value, 2), "unit": "iters/s", "h2d_bytes_per_step": int(img.nbytes),
+           "d2h_bytes_per_step": int(tr.info().site_buffer * 40 + 4), "psnr_db": round(e2e_psnr, 3),
+           "ms_per_fit": round(1e3 * float(np.mean(e2e_t)), 2)}
+    tr.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    if rank != 0:
+        return None
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": "iters/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": DATA,
+        "config": {"workload": WORKLOAD, "image": f"{WIDTH}x{HEIGHT}", "target_bpp": 1.0,
+                   "sites_start": 128000, "sites_final": final_sites, "iterations": iters,
+                   "step": "one whole fit (training loop timed; init outside)",
+                   "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas x{ws}"},
+        "mpix_per_s": round(value * WIDTH * HEIGHT / 1e6, 1),
+        "ms_per_iteration": round(total_ms / args.steps / iters, 5),
+        "psnr_db": round(psnr, 3),
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
+    return out
+
+
+def cpu_fit(img, seconds: float, threads: int):
+    """Oracle fit of the workload, iterations run until `seconds` pass (>= 2)."""
+    import orc
+    from sad_gb300 import _lib
+    from sad_gb300.config import train_config
+    cfg = train_config(log_freq=0)
+    sol = _lib.BppSolution()
+    import ctypes as C
+    _lib.call("sad_solve_target_bpp", 1.0, WIDTH, HEIGHT, cfg.n_sites, cfg.max_sites, cfg.iterations,
+              1, cfg.densify_start, cfg.densify_end, cfg.densify_freq, cfg.densify_percentile,
+              cfg.prune_during_densify, cfg.prune_start, cfg.prune_end, cfg.prune_freq,
+              cfg.prune_percentile, 65536, C.byref(sol))
+    cfg.prune_percentile, cfg.densify_percentile = sol.prune_percentile, sol.densify_percentile
+    f = orc.Fit(orc.fit_config_from(cfg, threads=threads), img)
+    t0 = time.perf_counter()
+    it = 0
+    while it < 2 or time.perf_counter() - t0 < seconds:
+        f.run(it, it + 1)
+        it += 1
+    dt = time.perf_counter() - t0
+    f.close()
+    return it, dt
+
+
+def cpu_baseline(seconds: float = 15.0):
+    from sad_gb300.synthetic import synthetic_image
+    threads = os.cpu_count() or 1
+    img = synthetic_image(WIDTH, HEIGHT, seed=0)
+    it, dt = cpu_fit(img, seconds, threads)
+    return {"value": round(it / dt, 4), "unit": "iters/s", "cores": threads, "kind": "port",
+            "sample": f"first {it} iterations of the same 1024x1024 fit ({dt:.1f} s, OpenMP x{threads})"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return None
+    from sad_gb300.synthetic import synthetic_image
+    import orc
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    img = synthetic_image(WIDTH, HEIGHT, seed=0)
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_fit(img, per_step / 4, threads)
+    its, secs = 0, 0.0
+    for _ in range(args.steps):
+        it, dt = cpu_fit(img, per_step, threads)
+        its += it
+        secs += dt
+    value = its / secs
+    return {"metric": METRIC, "value": round(value, 4), "unit": "iters/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": DATA, "impl": "reference",
+            "config": {"workload": WORKLOAD, "image": f"{WIDTH}x{HEIGHT}",
+                       "step": "a bounded sample (time-limited run of the fit's first iterations)"},
+            "cpu_baseline": {"value": round(value, 4), "unit": "iters/s", "cores": threads, "kind": "port",
+                             "sample": f"{its} iterations over {args.steps} steps, OpenMP x{threads}"},
+            "e2e": {"value": round(value, 4), "unit": "iters/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference's path is CUDA-only; this is the CPU restatement of its kernels"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    out = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,307 @@
+// gradients.cu -- fused training gradient: forward softmax, dL/dpred of the MSE (+ SSIM)
+// loss, per-site parameter gradients and the prune removal delta, accumulated per 16x16
+// tile in a shared-memory table with warp-merged inserts (accum.cuh).
+//
+// Semantics follow backends/cuda/src/gradients.cu:103-486 (computeGradientsTiledKernel):
+//   * masked pixels (mask <= 0) contribute nothing (the reference returns before its
+//     barrier; here they simply carry no keys, so every thread reaches the barrier);
+//   * a pixel whose candidates are all invalid contributes nothing;
+//   * l2 = 1 / max(l1, 1e-8) in the gradient algebra (gradients.cu:383);
+//   * the removal delta of a site is taken once per pixel with the site's summed weight
+//     over duplicate slots (gradients.cu:295-350).
+//
+// Tile mapping: 256 threads = 8 warps, each warp an 8x4 pixel patch, so the lanes of a
+// warp share most candidates and the warp merge collapses them before the shared table.
+#include "accum.cuh"
+#include "common.cuh"
+#include "host_common.h"
+#include "kernels.h"
+#include "sources.cuh"
+
+namespace sad {
+
+constexpr int kGradSlots = 512;
+
+__device__ __forceinline__ float luma(const float* __restrict__ p) {
+    return __ldg(p) * 0.299f + __ldg(p + 1) * 0.587f + __ldg(p + 2) * 0.114f;
+}
+
+// SSIM term of dL/dpred, backends/cuda/src/gradients.cu:258-292 (3x3 window, clamped taps)
+__device__ float ssim_dloss(const float* __restrict__ ren, const float* __restrict__ tgt, int x,
+                            int y, int w, int h) {
+    float mux = 0.f, muy = 0.f, ex2 = 0.f, ey2 = 0.f, exy = 0.f;
+    for (int dy = -1; dy <= 1; ++dy) {
+        int yy = clampi(y + dy, 0, h - 1);
+        for (int dx = -1; dx <= 1; ++dx) {
+            int xx = clampi(x + dx, 0, w - 1);
+            int i = 3 * (yy * w + xx);
+            float xv = luma(ren + i), yv = luma(tgt + i);
+            mux += xv;
+            muy += yv;
+            ex2 += xv * xv;
+            ey2 += yv * yv;
+            exy += xv * yv;
+        }
+    }
+    const float invn = 0.111111111f;
+    mux *= invn; muy *= invn; ex2 *= invn; ey2 *= invn; exy *= invn;
+    float sx2 = fmaxf(ex2 - mux * mux, 0.0f);
+    float sy2 = fmaxf(ey2 - muy * muy, 0.0f);
+    float sxy = exy - mux * muy;
+    float A = 2.0f * mux * muy + 0.0001f;
+    float B = 2.0f * sxy + 0.0009f;
+    float C = mux * mux + muy * muy + 0.0001f;
+    float D = sx2 + sy2 + 0.0009f;
+    float den = fmaxf(C * D, 1e-8f);
+    float num = A * B;
+    int p = 3 * (y * w + x);
+    float xk = luma(ren + p), yk = luma(tgt + p);
+    float dA = 2.0f * muy * invn;
+    float dB = 2.0f * (invn * (yk - muy));
+    float dC = 2.0f * mux * invn;
+    float dD = (2.0f * invn) * (xk - mux);
+    return (dA * B + A * dB) / den - num * (dC * D + C * dD) / (den * den);
+}
+
+template <bool kAoS, int NV>
+__device__ __forceinline__ void global_add(const GradParams& p, uint32_t key, const float (&v)[NV]) {
+    if (kAoS) {
+        float* o = p.aos12 + static_cast<size_t>(key) * 12;
+        red_add_v4(o, v[0], v[1], v[2], v[3]);
+        red_add_v4(o + 4, v[4], v[5], v[6], v[7]);
+        red_add_v4(o + 8, v[8], v[9], NV > 10 ? v[NV > 10 ? 10 : 0] : 0.0f, 0.0f);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 10; ++k) atomicAdd(p.soa[k] + key, v[k]);
+        if (NV > 10 && v[NV > 10 ? 10 : 0] != 0.0f) atomicAdd(p.removal + key, v[NV > 10 ? 10 : 0]);
+    }
+}
+
+template <class Src, bool kAoS, bool kRemoval, bool kSSIM>
+__global__ void __launch_bounds__(256) fused_gradients_kernel(GradParams prm, Src src) {
+    constexpr int NV = kRemoval ? 11 : 10;
+    __shared__ TileTable<NV, kGradSlots> table;
+    const int tid = threadIdx.x;
+    table.init(tid, 256);
+    __syncthreads();
+
+    const int lane = tid & 31, warp = tid >> 5;
+    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    const int y = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+    const int w = prm.width, h = prm.height;
+    const uint32_t n = prm.site_count;
+    const float inv_s2 = prm.inv_scale_sq;
+    const float inv_scale = sqrtf(inv_s2);
+    const float ux = static_cast<float>(x), uy = static_cast<float>(y);
+
+    uint32_t ids[kCand];
+    float wts[kCand];
+    uint32_t valid = 0, blend = 0;
+    float3 pred = make_float3(0.f, 0.f, 0.f), dLdp = make_float3(0.f, 0.f, 0.f);
+    float rem[kCand];
+#pragma unroll
+    for (int i = 0; i < kCand; ++i) {
+        ids[i] = kEmpty;
+        wts[i] = 0.0f;
+        rem[i] = 0.0f;
+    }
+
+    bool live = x < w && y < h;
+    int pix = live ? y * w + x : 0;
+    if (live && prm.mask) live = __ldg(prm.mask + pix) > 0.0f;
+    if (live) {
+        int ci = cand_index_for_pixel(x, y, w, h, prm.cand_width, prm.cand_height);
+        uint4 a = __ldg(reinterpret_cast<const uint4*>(prm.cand0) + ci);
+        uint4 b = __ldg(reinterpret_cast<const uint4*>(prm.cand1) + ci);
+        ids[0] = a.x; ids[1] = a.y; ids[2] = a.z; ids[3] = a.w;
+        ids[4] = b.x; ids[5] = b.y; ids[6] = b.z; ids[7] = b.w;
+        float logits[kCand];
+        float3 cols[kCand];
+        float mx = -INFINITY;
+#pragma unroll
+        for (int i = 0; i < kCand; ++i) {
+            logits[i] = -INFINITY;
+            cols[i] = make_float3(0.f, 0.f, 0.f);
+            if (ids[i] >= n) continue;
+            SiteGeom g;
+            src.load(ids[i], g, cols[i]);
+            if (g.px < 0.0f) continue;
+            valid |= 1u << i;
+            if (g.px >= 0.0f) blend |= 1u << i;
+            float tau = g.tau;
+            float d = dmix2(g, ux, uy, inv_s2, inv_scale);
+            logits[i] = -tau * d;
+            mx = fmaxf(mx, logits[i]);
+        }
+        if (!isinf(mx) || mx > 0.0f) {
+            float sum = 0.0f;
+#pragma unroll
+            for (int i = 0; i < kCand; ++i) {
+                wts[i] = expf(logits[i] - mx);
+                sum += wts[i];
+            }
+            float inv_sum = 1.0f / fmaxf(sum, 1e-8f);
+#pragma unroll
+            for (int i = 0; i < kCand; ++i) {
+                wts[i] *= inv_sum;
+                if (blend >> i & 1u) {
+                    pred.x += wts[i] * cols[i].x;
+                    pred.y += wts[i] * cols[i].y;
+                    pred.z += wts[i] * cols[i].z;
+                }
+            }
+            const float* t = prm.target + 3 * pix;
+            float3 tgt = make_float3(__ldg(t), __ldg(t + 1), __ldg(t + 2));
+            dLdp = make_float3(2.0f * (pred.x - tgt.x), 2.0f * (pred.y - tgt.y),
+                               2.0f * (pred.z - tgt.z));
+            if (kSSIM) {
+                float ds = ssim_dloss(prm.rendered, prm.target, x, y, w, h);
+                float k = -prm.ssim_weight * ds;
+                dLdp.x += k * 0.299f;
+                dLdp.y += k * 0.587f;
+                dLdp.z += k * 0.114f;
+            }
+            if (kRemoval) {
+                // first slot of each distinct valid site carries its removal delta
+#pragma unroll
+                for (int i = 0; i < kCand; ++i) {
+                    if (!(valid >> i & 1u)) continue;
+                    bool first = true;
+#pragma unroll
+                    for (int j = 0; j < i; ++j) first &= !((valid >> j & 1u) && ids[j] == ids[i]);
+                    if (!first) continue;
+                    float wt = 0.0f;
+#pragma unroll
+                    for (int j = i; j < kCand; ++j)
+                        if ((valid >> j & 1u) && ids[j] == ids[i]) wt += wts[j];
+                    if (!(wt > 0.0f)) continue;
+                    float keep = 1.0f - wt;
+                    float delta;
+                    if (keep < 1e-4f) {
+                        delta = 1.0e6f;
+                    } else {
+                        float3 c = cols[i];
+                        float3 pk = make_float3((pred.x - wt * c.x) / keep, (pred.y - wt * c.y) / keep,
+                                                (pred.z - wt * c.z) / keep);
+                        float3 df = make_float3(pred.x - tgt.x, pred.y - tgt.y, pred.z - tgt.z);
+                        float3 dk = make_float3(pk.x - tgt.x, pk.y - tgt.y, pk.z - tgt.z);
+                        delta = (dk.x * dk.x + dk.y * dk.y + dk.z * dk.z) -
+                                (df.x * df.x + df.y * df.y + df.z * df.z);
+                    }
+                    rem[i] = delta;
+                }
+            }
+        } else {
+            valid = 0;
+        }
+    }
+
+#pragma unroll
+    for (int i = 0; i < kCand; ++i) {
+        float v[NV];
+        uint32_t key = kEmpty;
+        if (valid >> i & 1u) {
+            SiteGeom g;
+            float3 col;
+            src.load(ids[i], g, col);
+            float o[10];
+            candidate_grads(g, col, ux, uy, inv_s2, inv_scale, wts[i], dLdp, pred, true, o);
+#pragma unroll
+            for (int k = 0; k < 10; ++k) v[k] = o[k];
+            if (NV > 10) v[NV - 1] = rem[i];
+            key = ids[i];
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) v[k] = 0.0f;
+        }
+        bool leader = warp_merge_by_key<NV>(key, v);
+        if (leader && key != kEmpty) {
+            if (!table.add(key, v)) global_add<kAoS, NV>(prm, key, v);
+        }
+    }
+    __syncthreads();
+    for (int s = tid; s < kGradSlots; s += 256) {
+        uint32_t key = table.keys[s];
+        if (key == kEmpty) continue;
+        float v[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) v[k] = table.vals[k][s];
+        global_add<kAoS, NV>(prm, key, v);
+    }
+}
+
+template <class Src, bool kAoS>
+static void dispatch_gradients(const GradParams& p, Src src, cudaStream_t st) {
+    dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
+    bool rem = p.compute_removal != 0;
+    bool ssim = p.ssim_weight > 0.0f;
+    if (rem && ssim)
+        fused_gradients_kernel<Src, kAoS, true, true><<<grid, 256, 0, st>>>(p, src);
+    else if (rem)
+        fused_gradients_kernel<Src, kAoS, true, false><<<grid, 256, 0, st>>>(p, src);
+    else if (ssim)
+        fused_gradients_kernel<Src, kAoS, false, true><<<grid, 256, 0, st>>>(p, src);
+    else
+        fused_gradients_kernel<Src, kAoS, false, false><<<grid, 256, 0, st>>>(p, src);
+    note_launches(1);
+}
+
+void launch_gradients_raw(const GradParams& p, const Site* sites, cudaStream_t st) {
+    if (p.aos12)
+        dispatch_gradients<RawSites, true>(p, RawSites{sites}, st);
+    else
+        dispatch_gradients<RawSites, false>(p, RawSites{sites}, st);
+}
+
+void launch_gradients_prepared(const GradParams& p, const SiteGeom* geom, const SiteColor* color,
+                               cudaStream_t st) {
+    if (p.aos12)
+        dispatch_gradients<PreparedSites, true>(p, PreparedSites{geom, color}, st);
+    else
+        dispatch_gradients<PreparedSites, false>(p, PreparedSites{geom, color}, st);
+}
+
+}  // namespace sad
+
+using namespace sad;
+
+extern "C" sad_status_t sad_compute_gradients_tiled(
+    const uint32_t* cand0, const uint32_t* cand1, const float* target, const float* rendered,
+    const float* mask, float* grad_pos_x, float* grad_pos_y, float* grad_log_tau,
+    float* grad_radius, float* grad_color_r, float* grad_color_g, float* grad_color_b,
+    float* grad_dir_x, float* grad_dir_y, float* grad_log_aniso, const float* sites,
+    float inv_scale_sq, uint32_t site_count, float* removal_delta, uint32_t compute_removal,
+    float ssim_weight, int width, int height, int cand_width, int cand_height,
+    sad_stream_t stream) {
+    clear_error();
+    SAD_REQUIRE(width > 0 && height > 0, "sad_compute_gradients_tiled: invalid image size");
+    SAD_REQUIRE(cand_width > 0 && cand_height > 0, "sad_compute_gradients_tiled: invalid cand size");
+    SAD_REQUIRE(cand0 && cand1 && target, "sad_compute_gradients_tiled: null input");
+    SAD_REQUIRE(ssim_weight <= 0.0f || rendered, "sad_compute_gradients_tiled: SSIM needs rendered");
+    SAD_REQUIRE(grad_pos_x && grad_pos_y && grad_log_tau && grad_radius && grad_color_r &&
+                    grad_color_g && grad_color_b && grad_dir_x && grad_dir_y && grad_log_aniso,
+                "sad_compute_gradients_tiled: null gradient array");
+    SAD_REQUIRE(!compute_removal || removal_delta, "sad_compute_gradients_tiled: null removal_delta");
+    SAD_REQUIRE(sites || site_count == 0, "sad_compute_gradients_tiled: null sites");
+    GradParams p{};
+    p.cand0 = cand0;
+    p.cand1 = cand1;
+    p.target = target;
+    p.rendered = rendered;
+    p.mask = mask;
+    p.inv_scale_sq = inv_scale_sq;
+    p.site_count = site_count;
+    p.ssim_weight = ssim_weight;
+    p.width = width;
+    p.height = height;
+    p.cand_width = cand_width;
+    p.cand_height = cand_height;
+    float* g[10] = {grad_pos_x, grad_pos_y, grad_log_tau, grad_radius, grad_color_r,
+                    grad_color_g, grad_color_b, grad_dir_x, grad_dir_y, grad_log_aniso};
+    for (int k = 0; k < 10; ++k) p.soa[k] = g[k];
+    p.removal = removal_delta;
+    p.aos12 = nullptr;
+    p.compute_removal = compute_removal ? 1 : 0;
+    launch_gradients_raw(p, reinterpret_cast<const Site*>(sites), as_stream(stream));
+    return check_launch("sad_compute_gradients_tiled");
+}

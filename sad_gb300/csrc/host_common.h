@@ -1,0 +1,65 @@
+// host_common.h -- error reporting shared by the C-ABI entry points.
+//
+// Every entry point returns a sad_status_t.  On failure the message is kept in a
+// thread-local buffer readable through sad_last_error().  Launch errors are
+// collected with cudaGetLastError() right after each launch, so a bad launch
+// configuration is reported by the call that made it.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "../../include/sad_gb300.h"
+
+namespace sad {
+
+void set_error(const char* fmt, ...);
+void clear_error();
+
+inline sad_status_t fail(sad_status_t code, const char* msg) {
+    set_error("%s", msg);
+    return code;
+}
+
+inline sad_status_t check_launch(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("%s: %s", what, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? SAD_ERR_OUT_OF_MEMORY : SAD_ERR_CUDA;
+    }
+    return SAD_OK;
+}
+
+inline sad_status_t check_cuda(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        set_error("%s: %s", what, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? SAD_ERR_OUT_OF_MEMORY : SAD_ERR_CUDA;
+    }
+    return SAD_OK;
+}
+
+inline cudaStream_t as_stream(sad_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline unsigned blocks_for(size_t n, unsigned threads) {
+    return static_cast<unsigned>((n + threads - 1) / threads);
+}
+
+// Counts kernel launches issued by this library (read by the benchmark to report how
+// many of its own kernels ran in a timed region).
+void note_launches(uint64_t n);
+
+}  // namespace sad
+
+#define SAD_REQUIRE(cond, msg)                                      \
+    do {                                                            \
+        if (!(cond)) return ::sad::fail(SAD_ERR_INVALID_ARGUMENT, msg); \
+    } while (0)
+
+#define SAD_TRY(expr)                        \
+    do {                                     \
+        sad_status_t st_ = (expr);           \
+        if (st_ != SAD_OK) return st_;       \
+    } while (0)

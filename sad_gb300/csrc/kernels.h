@@ -1,0 +1,156 @@
+// kernels.h -- internal launch functions shared by the C-ABI wrappers and the trainer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace sad {
+
+struct VptParams {
+    const uint32_t* in0;
+    const uint32_t* in1;
+    uint32_t* out0;
+    uint32_t* out1;
+    uint32_t site_count;
+    uint32_t step;       // packed (jump << 16) | index, used when state == nullptr
+    uint32_t step_high;  // index >> 16
+    float inv_scale_sq;
+    float radius_scale;
+    uint32_t radius_probes;
+    uint32_t inject_count;
+    const uint32_t* hilbert_order;
+    const uint32_t* hilbert_pos;
+    uint32_t hilbert_probes;
+    uint32_t hilbert_window;
+    int cand_downscale;
+    int target_width, target_height;
+    int width, height;  // candidate field
+    // trainer mode: step taken from state->vpt_pass + pass_offset
+    const DevState* state;
+    uint32_t pass_offset;
+    uint32_t pow2, stages;
+};
+
+// render.cu
+void launch_prepare_sites(const Site* sites, SiteGeom* geom, SiteColor* color, uint32_t n,
+                          cudaStream_t st);
+void launch_render_raw(const uint32_t* c0, const uint32_t* c1, float* out, const Site* sites,
+                       float inv_s2, uint32_t n, int w, int h, int cw, int ch, cudaStream_t st);
+void launch_render_prepared(const uint32_t* c0, const uint32_t* c1, float* out,
+                            const SiteGeom* geom, const SiteColor* color, float inv_s2,
+                            uint32_t n, int w, int h, int cw, int ch, cudaStream_t st);
+void launch_init_candidates(uint32_t* c0, uint32_t* c1, uint32_t n, uint32_t seed, int per_pixel,
+                            int w, int h, cudaStream_t st);
+void launch_clear_candidates(uint32_t* c0, uint32_t* c1, int w, int h, cudaStream_t st);
+void launch_render_backward_raw(const uint32_t* c0, const uint32_t* c1, const float* grad_rgb,
+                                float* grad_sites, const Site* sites, float inv_s2, uint32_t n,
+                                int w, int h, int cw, int ch, cudaStream_t st);
+
+// candidates.cu
+void launch_pack_sites(const Site* sites, uint16_t* packed, uint32_t n, cudaStream_t st);
+void launch_pack_geom(const Site* sites, SiteGeom* out, uint32_t n, cudaStream_t st);
+void launch_vpt_packed(const VptParams& prm, const uint16_t* packed, cudaStream_t st);
+void launch_vpt_geom(const VptParams& prm, const SiteGeom* geom, cudaStream_t st);
+void launch_jfa_seed(uint32_t* cand0, const Site* sites, uint32_t n, int w, int h, int ds,
+                     cudaStream_t st);
+void launch_jfa_flood_raw(const uint32_t* in0, uint32_t* out0, const Site* sites, uint32_t n,
+                          uint32_t step, float inv_s2, int w, int h, int ds, int tw, int th,
+                          cudaStream_t st);
+void launch_jfa_flood_geom(const uint32_t* in0, uint32_t* out0, const SiteGeom* geom, uint32_t n,
+                           uint32_t step, float inv_s2, int w, int h, int ds, int tw, int th,
+                           cudaStream_t st);
+uint32_t host_jump_step_for_index(uint32_t idx, int w, int h);
+void jump_schedule_constants(int w, int h, uint32_t* pow2, uint32_t* stages);
+
+// gradients.cu
+struct GradParams {
+    const uint32_t* cand0;
+    const uint32_t* cand1;
+    const float* target;    // [H,W,3]
+    const float* rendered;  // [H,W,3], read only when ssim_weight > 0
+    const float* mask;      // [H,W] or nullptr
+    float inv_scale_sq;
+    uint32_t site_count;
+    float ssim_weight;
+    int width, height, cand_width, cand_height;
+    // outputs: either 10 SoA arrays (+ removal) or one [N][12] array (slot 10 = removal)
+    float* soa[10];
+    float* removal;
+    float* aos12;
+    int compute_removal;
+};
+void launch_gradients_raw(const GradParams& p, const Site* sites, cudaStream_t st);
+void launch_gradients_prepared(const GradParams& p, const SiteGeom* geom, const SiteColor* color,
+                               cudaStream_t st);
+
+// optim.cu
+void launch_tau_diffuse_raw(const uint32_t* c0, const uint32_t* c1, const Site* sites,
+                            const float* raw, const float* gin, float* gout, uint32_t n,
+                            float lambda, int w, int h, int ds, cudaStream_t st);
+// trainer form: log-tau gradient read from aos12 slot 2 (raw and first input), lambda from
+// the iteration counter
+void launch_tau_diffuse_train(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
+                              const float* aos12, const float* gin, int gin_stride, float* gout,
+                              uint32_t n, const DevState* state, int iterations, int w, int h,
+                              int ds, cudaStream_t st);
+struct AdamHyper {
+    float lr_pos, lr_tau, lr_radius, lr_color, lr_dir, lr_aniso;
+    float beta1, beta2, eps;
+};
+void launch_adam_soa(Site* sites, float* adam, const float* const g[10], const AdamHyper& hp,
+                     uint32_t t, uint32_t n, int w, int h, cudaStream_t st);
+// trainer form: reads aos12 grads (log-tau from tau_grad), zeroes slots 0-9, writes the
+// prepared records; t = state->iter + 1
+void launch_adam_train(Site* sites, float* adam, float* aos12, const float* tau_grad,
+                       SiteGeom* geom, SiteColor* color, const AdamHyper& hp,
+                       const DevState* state, uint32_t n, int w, int h, cudaStream_t st);
+void launch_clear_f32(float* buf, size_t count, cudaStream_t st);
+void launch_advance_state(DevState* state, uint32_t vpt_passes, cudaStream_t st);
+
+// sort.cu
+size_t radix_sort_temp_bytes(uint32_t count);
+void launch_radix_sort(uint32_t* pairs, uint32_t count, uint32_t max_key_exclusive, void* temp,
+                       cudaStream_t st);
+// exclusive scan of `count` words in place by one CTA; *total (nullable) = sum
+void launch_scan_single(uint32_t* data, uint32_t count, uint32_t* total, cudaStream_t st);
+
+// topology.cu
+void launch_densify_pairs(const Site* sites, const float* mass, const float* energy,
+                          uint32_t* pairs, uint32_t n, float min_mass, float alpha,
+                          uint32_t pair_count, cudaStream_t st);
+void launch_prune_pairs(const Site* sites, const float* removal, int removal_stride,
+                        uint32_t* pairs, uint32_t n, float delta_norm, uint32_t pair_count,
+                        cudaStream_t st);
+void launch_write_indices(const uint32_t* pairs, uint32_t* idx, uint32_t k, cudaStream_t st);
+void launch_prune_by_index(Site* sites, const uint32_t* idx, uint32_t k, cudaStream_t st);
+// trainer form: prune the first prune_k[state->iter] entries of sorted pairs, also in geom
+void launch_prune_sorted_train(Site* sites, SiteGeom* geom, const uint32_t* pairs,
+                               const uint32_t* prune_k, const DevState* state, uint32_t max_k,
+                               cudaStream_t st);
+void launch_split(Site* sites, float* adam, const uint32_t* split_idx, uint32_t num,
+                  const float* const stats[7], uint32_t cur, const float* target, int w, int h,
+                  cudaStream_t st);
+void launch_site_stats(const uint32_t* c0, const uint32_t* c1, const float* target,
+                       const float* mask, const Site* sites, float inv_s2, uint32_t n,
+                       float* const out[8], int w, int h, int cw, int ch, cudaStream_t st);
+void launch_hilbert_pairs(const Site* sites, uint32_t* pairs, uint32_t n, uint32_t padded, int w,
+                          int h, int bits, cudaStream_t st);
+void launch_hilbert_order(const uint32_t* pairs, uint32_t* order, uint32_t* pos, uint32_t n,
+                          cudaStream_t st);
+void launch_mse(const float* ren, const float* tgt, const float* mask, float* acc, int w, int h,
+                cudaStream_t st);
+void launch_ssim(const float* ren, const float* tgt, const float* mask, float* acc, int w, int h,
+                 cudaStream_t st);
+void launch_count_active(const Site* sites, uint32_t* count, uint32_t n, cudaStream_t st);
+size_t init_temp_bytes(uint32_t n);
+cudaError_t run_init_gradient_weighted(Site* sites, uint32_t n, const float* target,
+                                       const float* mask, float thr, uint32_t max_attempts,
+                                       float init_log_tau, float init_radius, int w, int h,
+                                       void* temp, cudaStream_t st);
+
+}  // namespace sad

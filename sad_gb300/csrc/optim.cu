@@ -1,0 +1,383 @@
+// optim.cu -- per-site optimisation: log-tau gradient diffusion, Adam, gradient clears.
+//
+// Trainer forms keep every iteration-dependent scalar on the device (DevState), so one
+// captured CUDA graph per iteration kind is replayed for the whole fit:
+//   * tau diffusion: lambda = 0.05 (0.1 + 0.9 iter / iters), the host formula of
+//     backends/cuda/src/sad_cuda.cu:2339-2340, evaluated without contraction like an
+//     x86 host build would;
+//   * Adam: t = iter + 1 (sad_cuda.cu:2369-2380), fused with the gradient clear
+//     (adam.cu:183-209) and with the refresh of the prepared SiteGeom/SiteColor records
+//     the per-pixel kernels gather.
+#include "common.cuh"
+#include "host_common.h"
+#include "kernels.h"
+
+namespace sad {
+
+// ---------------------------------------------------------------------------
+// tau diffusion (backends/cuda/src/tau_diffusion.cu:27-89)
+// ---------------------------------------------------------------------------
+template <class PosFn>
+__device__ __forceinline__ float tau_diffuse_one(uint32_t i, const uint4* __restrict__ c0,
+                                                 const uint4* __restrict__ c1, PosFn pos,
+                                                 const float* __restrict__ raw, int raw_stride,
+                                                 const float* __restrict__ gin, int gin_stride,
+                                                 uint32_t n, float lambda, int w, int h, int ds) {
+    float2 sp = pos(i);
+    if (lambda <= 0.0f || sp.x < 0.0f) return gin[static_cast<size_t>(i) * gin_stride];
+    float inv = 1.0f / fmaxf(static_cast<float>(ds), 1.0f);
+    int px = clampi(static_cast<int>(sp.x * inv + 0.5f), 0, w - 1);
+    int py = clampi(static_cast<int>(sp.y * inv + 0.5f), 0, h - 1);
+    int p = py * w + px;
+    uint4 a = __ldg(c0 + p), b = __ldg(c1 + p);
+    uint32_t ids[kCand] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    float sum = 0.0f;
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kCand; ++k) {
+        uint32_t m = ids[k];
+        if (m >= n || m == i) continue;
+        bool seen = false;
+#pragma unroll
+        for (int j = 0; j < k; ++j) seen |= ids[j] == m;
+        if (seen) continue;
+        if (pos(m).x < 0.0f) continue;
+        sum += gin[static_cast<size_t>(m) * gin_stride];
+        cnt += 1;
+    }
+    float diag = 1.0f + lambda * static_cast<float>(cnt);
+    return (raw[static_cast<size_t>(i) * raw_stride] + lambda * sum) / diag;
+}
+
+__global__ void tau_diffuse_raw_kernel(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
+                                       const Site* __restrict__ sites, const float* __restrict__ raw,
+                                       const float* __restrict__ gin, float* __restrict__ gout,
+                                       uint32_t n, float lambda, int w, int h, int ds) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    auto pos = [sites](uint32_t k) { return make_float2(__ldg(&sites[k].px), __ldg(&sites[k].py)); };
+    gout[i] = tau_diffuse_one(i, c0, c1, pos, raw, 1, gin, 1, n, lambda, w, h, ds);
+}
+
+void launch_tau_diffuse_raw(const uint32_t* c0, const uint32_t* c1, const Site* sites,
+                            const float* raw, const float* gin, float* gout, uint32_t n,
+                            float lambda, int w, int h, int ds, cudaStream_t st) {
+    if (n == 0) return;
+    tau_diffuse_raw_kernel<<<blocks_for(n, 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), sites, raw, gin,
+        gout, n, lambda, w, h, ds);
+    note_launches(1);
+}
+
+__device__ __forceinline__ float tau_lambda(uint32_t iter, int iterations) {
+    float blend = __fdiv_rn(static_cast<float>(iter), static_cast<float>(max(1, iterations)));
+    return __fmul_rn(0.05f, __fadd_rn(0.1f, __fmul_rn(0.9f, blend)));
+}
+
+__global__ void tau_diffuse_train_kernel(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
+                                         const SiteGeom* __restrict__ geom,
+                                         const float* __restrict__ aos12,
+                                         const float* __restrict__ gin, int gin_stride,
+                                         float* __restrict__ gout, uint32_t n,
+                                         const DevState* __restrict__ state, int iterations, int w,
+                                         int h, int ds) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float lambda = tau_lambda(state->iter, iterations);
+    auto pos = [geom](uint32_t k) {
+        float2 v = __ldg(reinterpret_cast<const float2*>(geom + k));
+        return v;
+    };
+    gout[i] = tau_diffuse_one(i, c0, c1, pos, aos12 + 2, 12, gin, gin_stride, n, lambda, w, h, ds);
+}
+
+void launch_tau_diffuse_train(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
+                              const float* aos12, const float* gin, int gin_stride, float* gout,
+                              uint32_t n, const DevState* state, int iterations, int w, int h,
+                              int ds, cudaStream_t st) {
+    if (n == 0) return;
+    tau_diffuse_train_kernel<<<blocks_for(n, 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), geom, aos12, gin,
+        gin_stride, gout, n, state, iterations, w, h, ds);
+    note_launches(1);
+}
+
+// ---------------------------------------------------------------------------
+// Adam (backends/cuda/src/adam.cu:5-180)
+// ---------------------------------------------------------------------------
+struct AdamSlots {  // the 20-float per-site state
+    float v[20];
+};
+
+__device__ __forceinline__ void adam_load(const float* __restrict__ a, uint32_t i, AdamSlots& s) {
+    const float4* q = reinterpret_cast<const float4*>(a + static_cast<size_t>(i) * 20);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        float4 t = q[k];
+        s.v[4 * k] = t.x; s.v[4 * k + 1] = t.y; s.v[4 * k + 2] = t.z; s.v[4 * k + 3] = t.w;
+    }
+}
+
+__device__ __forceinline__ void adam_store(float* __restrict__ a, uint32_t i, const AdamSlots& s) {
+    float4* q = reinterpret_cast<float4*>(a + static_cast<size_t>(i) * 20);
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        q[k] = make_float4(s.v[4 * k], s.v[4 * k + 1], s.v[4 * k + 2], s.v[4 * k + 3]);
+}
+
+// One Adam step of one active site.  g[] = the 10 normalised gradients in site order.
+__device__ __forceinline__ void adam_site(Site& s, AdamSlots& a, const float (&g)[10],
+                                          const AdamHyper& hp, float c1, float c2, int w, int h) {
+    const float b1 = hp.beta1, b2 = hp.beta2, eps = hp.eps;
+    // position: isotropic Adam
+    a.v[0] = b1 * a.v[0] + (1.0f - b1) * g[0];
+    a.v[1] = b1 * a.v[1] + (1.0f - b1) * g[1];
+    float g2p = g[0] * g[0] + g[1] * g[1];
+    a.v[2] = b2 * a.v[2] + (1.0f - b2) * g2p;
+    {
+        float mh0 = a.v[0] * c1, mh1 = a.v[1] * c1;
+        float vh = a.v[2] * c2;
+        float idn = 1.0f / (sqrtf(vh) + eps);
+        float st0 = hp.lr_pos * mh0 * idn, st1 = hp.lr_pos * mh1 * idn;
+        s.px -= st0;
+        s.py -= st1;
+        s.px = clampf(s.px, 0.0f, static_cast<float>(w - 1));
+        s.py = clampf(s.py, 0.0f, static_cast<float>(h - 1));
+    }
+    // log_tau
+    a.v[3] = b1 * a.v[3] + (1.0f - b1) * g[2];
+    a.v[4] = b2 * a.v[4] + (1.0f - b2) * (g[2] * g[2]);
+    s.log_tau -= hp.lr_tau * (a.v[3] * c1) / (sqrtf(a.v[4] * c2) + eps);
+    // radius
+    a.v[5] = b1 * a.v[5] + (1.0f - b1) * g[3];
+    a.v[6] = b2 * a.v[6] + (1.0f - b2) * (g[3] * g[3]);
+    s.radius -= hp.lr_radius * (a.v[5] * c1) / (sqrtf(a.v[6] * c2) + eps);
+    s.radius = clampf(s.radius, 1.0f, 512.0f);
+    // colour, per channel
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        a.v[7 + c] = b1 * a.v[7 + c] + (1.0f - b1) * g[4 + c];
+        a.v[10 + c] = b2 * a.v[10 + c] + (1.0f - b2) * (g[4 + c] * g[4 + c]);
+    }
+    float st_r = hp.lr_color * (a.v[7] * c1) / (sqrtf(a.v[10] * c2) + eps);
+    float st_g = hp.lr_color * (a.v[8] * c1) / (sqrtf(a.v[11] * c2) + eps);
+    float st_b = hp.lr_color * (a.v[9] * c1) / (sqrtf(a.v[12] * c2) + eps);
+    s.r = clampf(s.r - st_r, 0.0f, 1.0f);
+    s.g = clampf(s.g - st_g, 0.0f, 1.0f);
+    s.b = clampf(s.b - st_b, 0.0f, 1.0f);
+    // direction: tangent-space isotropic Adam, renormalised
+    {
+        float dx = s.dx, dy = s.dy;
+        float gd = g[7] * dx + g[8] * dy;
+        float gtx = g[7] - dx * gd, gty = g[8] - dy * gd;
+        a.v[13] = b1 * a.v[13] + (1.0f - b1) * gtx;
+        a.v[14] = b1 * a.v[14] + (1.0f - b1) * gty;
+        float g2d = gtx * gtx + gty * gty;
+        a.v[15] = b2 * a.v[15] + (1.0f - b2) * g2d;
+        float mh0 = a.v[13] * c1, mh1 = a.v[14] * c1;
+        float vh = a.v[15] * c2;
+        float idn = 1.0f / (sqrtf(vh) + eps);
+        float nx = dx - hp.lr_dir * mh0 * idn, ny = dy - hp.lr_dir * mh1 * idn;
+        float l2 = nx * nx + ny * ny;
+        if (l2 < 1e-12f) {
+            nx = 1.0f;
+            ny = 0.0f;
+        } else {
+            float il = rsqrtf(l2);
+            nx *= il;
+            ny *= il;
+        }
+        s.dx = nx;
+        s.dy = ny;
+    }
+    // log_aniso
+    a.v[16] = b1 * a.v[16] + (1.0f - b1) * g[9];
+    a.v[17] = b2 * a.v[17] + (1.0f - b2) * (g[9] * g[9]);
+    s.log_aniso -= hp.lr_aniso * (a.v[16] * c1) / (sqrtf(a.v[17] * c2) + eps);
+    s.log_aniso = clampf(s.log_aniso, -4.0f, 4.0f);
+}
+
+__device__ __forceinline__ Site site_load(const Site* __restrict__ sites, uint32_t i) {
+    const float2* q = reinterpret_cast<const float2*>(sites + i);
+    float2 a = q[0], b = q[1], c = q[2], d = q[3], e = q[4];
+    Site s;
+    s.px = a.x; s.py = a.y; s.log_tau = b.x; s.radius = b.y; s.r = c.x; s.g = c.y;
+    s.b = d.x; s.dx = d.y; s.dy = e.x; s.log_aniso = e.y;
+    return s;
+}
+
+__device__ __forceinline__ void site_store(Site* __restrict__ sites, uint32_t i, const Site& s) {
+    float2* q = reinterpret_cast<float2*>(sites + i);
+    q[0] = make_float2(s.px, s.py);
+    q[1] = make_float2(s.log_tau, s.radius);
+    q[2] = make_float2(s.r, s.g);
+    q[3] = make_float2(s.b, s.dx);
+    q[4] = make_float2(s.dy, s.log_aniso);
+}
+
+struct SoaGrads {
+    const float* g[10];
+};
+
+__global__ void adam_soa_kernel(Site* __restrict__ sites, float* __restrict__ adam, SoaGrads gr,
+                                AdamHyper hp, uint32_t t, uint32_t n, int w, int h) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float norm = 1.0f / static_cast<float>(w * h);
+    float g[10];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) g[k] = gr.g[k][i] * norm;
+    Site s = site_load(sites, i);
+    if (s.px < 0.0f) return;
+    float tt = static_cast<float>(t);
+    float c1 = 1.0f / (1.0f - powf(hp.beta1, tt));
+    float c2 = 1.0f / (1.0f - powf(hp.beta2, tt));
+    AdamSlots a;
+    adam_load(adam, i, a);
+    adam_site(s, a, g, hp, c1, c2, w, h);
+    adam_store(adam, i, a);
+    site_store(sites, i, s);
+}
+
+void launch_adam_soa(Site* sites, float* adam, const float* const g[10], const AdamHyper& hp,
+                     uint32_t t, uint32_t n, int w, int h, cudaStream_t st) {
+    if (n == 0) return;
+    SoaGrads gr;
+    for (int k = 0; k < 10; ++k) gr.g[k] = g[k];
+    adam_soa_kernel<<<blocks_for(n, 256), 256, 0, st>>>(sites, adam, gr, hp, t, n, w, h);
+    note_launches(1);
+}
+
+__global__ void adam_train_kernel(Site* __restrict__ sites, float* __restrict__ adam,
+                                  float* __restrict__ aos12, const float* __restrict__ tau_grad,
+                                  SiteGeom* __restrict__ geom, SiteColor* __restrict__ color,
+                                  AdamHyper hp, const DevState* __restrict__ state, uint32_t n,
+                                  int w, int h) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float norm = 1.0f / static_cast<float>(w * h);
+    float4* gq = reinterpret_cast<float4*>(aos12 + static_cast<size_t>(i) * 12);
+    float4 g0 = gq[0], g1 = gq[1];
+    float2 g2 = *reinterpret_cast<float2*>(aos12 + static_cast<size_t>(i) * 12 + 8);
+    // consume and clear slots 0-9 (slot 10, the removal delta, is read by the prune step)
+    gq[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    gq[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    *reinterpret_cast<float2*>(aos12 + static_cast<size_t>(i) * 12 + 8) = make_float2(0.f, 0.f);
+    float g[10] = {g0.x * norm, g0.y * norm, tau_grad[i] * norm, g0.w * norm, g1.x * norm,
+                   g1.y * norm, g1.z * norm, g1.w * norm, g2.x * norm, g2.y * norm};
+    Site s = site_load(sites, i);
+    if (s.px < 0.0f) return;
+    float tt = static_cast<float>(state->iter + 1u);
+    float c1 = 1.0f / (1.0f - powf(hp.beta1, tt));
+    float c2 = 1.0f / (1.0f - powf(hp.beta2, tt));
+    AdamSlots a;
+    adam_load(adam, i, a);
+    adam_site(s, a, g, hp, c1, c2, w, h);
+    adam_store(adam, i, a);
+    site_store(sites, i, s);
+    store_geom(geom, i, make_geom(s.px, s.py, s.log_tau, s.radius, s.dx, s.dy, s.log_aniso));
+    reinterpret_cast<float4*>(color)[i] = make_float4(s.r, s.g, s.b, 0.0f);
+}
+
+void launch_adam_train(Site* sites, float* adam, float* aos12, const float* tau_grad,
+                       SiteGeom* geom, SiteColor* color, const AdamHyper& hp,
+                       const DevState* state, uint32_t n, int w, int h, cudaStream_t st) {
+    if (n == 0) return;
+    adam_train_kernel<<<blocks_for(n, 256), 256, 0, st>>>(sites, adam, aos12, tau_grad, geom, color,
+                                                          hp, state, n, w, h);
+    note_launches(1);
+}
+
+// ---------------------------------------------------------------------------
+// clears and the iteration counter
+// ---------------------------------------------------------------------------
+__global__ void clear_f32_kernel(float* __restrict__ buf, size_t count) {
+    size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
+    size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    for (; i < count; i += stride) buf[i] = 0.0f;
+}
+
+void launch_clear_f32(float* buf, size_t count, cudaStream_t st) {
+    if (count == 0) return;
+    unsigned blocks = static_cast<unsigned>(std::min<size_t>((count + 255) / 256, 152 * 16));
+    clear_f32_kernel<<<blocks, 256, 0, st>>>(buf, count);
+    note_launches(1);
+}
+
+__global__ void clear10_kernel(SoaGrads g, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+#pragma unroll
+    for (int k = 0; k < 10; ++k) const_cast<float*>(g.g[k])[i] = 0.0f;
+}
+
+__global__ void advance_state_kernel(DevState* state, uint32_t vpt_passes) {
+    state->iter += 1u;
+    state->vpt_pass += vpt_passes;
+}
+
+void launch_advance_state(DevState* state, uint32_t vpt_passes, cudaStream_t st) {
+    advance_state_kernel<<<1, 1, 0, st>>>(state, vpt_passes);
+    note_launches(1);
+}
+
+}  // namespace sad
+
+using namespace sad;
+
+extern "C" sad_status_t sad_tau_diffuse(const uint32_t* cand0, const uint32_t* cand1,
+                                        const float* sites, const float* grad_raw,
+                                        const float* grad_in, float* grad_out, uint32_t site_count,
+                                        float lambda, int width, int height, int cand_downscale,
+                                        sad_stream_t stream) {
+    clear_error();
+    SAD_REQUIRE(width > 0 && height > 0, "sad_tau_diffuse: invalid cand size");
+    SAD_REQUIRE(site_count == 0 || (cand0 && cand1 && sites && grad_raw && grad_in && grad_out),
+                "sad_tau_diffuse: null buffer");
+    SAD_REQUIRE(grad_in != grad_out, "sad_tau_diffuse: grad_in and grad_out must differ");
+    launch_tau_diffuse_raw(cand0, cand1, reinterpret_cast<const Site*>(sites), grad_raw, grad_in,
+                           grad_out, site_count, lambda, width, height, cand_downscale,
+                           as_stream(stream));
+    return check_launch("sad_tau_diffuse");
+}
+
+extern "C" sad_status_t sad_adam_update(float* sites, float* adam, const float* gpx,
+                                        const float* gpy, const float* glt, const float* grad,
+                                        const float* gr, const float* gg, const float* gb,
+                                        const float* gdx, const float* gdy, const float* gla,
+                                        float lr_pos, float lr_tau, float lr_radius,
+                                        float lr_color, float lr_dir, float lr_aniso, float beta1,
+                                        float beta2, float eps, uint32_t t, uint32_t site_count,
+                                        int width, int height, sad_stream_t stream) {
+    clear_error();
+    SAD_REQUIRE(width > 0 && height > 0, "sad_adam_update: invalid image size");
+    SAD_REQUIRE(site_count == 0 || (sites && adam && gpx && gpy && glt && grad && gr && gg && gb &&
+                                    gdx && gdy && gla),
+                "sad_adam_update: null buffer");
+    SAD_REQUIRE((reinterpret_cast<uintptr_t>(adam) & 15u) == 0, "sad_adam_update: adam must be 16-byte aligned");
+    AdamHyper hp{lr_pos, lr_tau, lr_radius, lr_color, lr_dir, lr_aniso, beta1, beta2, eps};
+    const float* g[10] = {gpx, gpy, glt, grad, gr, gg, gb, gdx, gdy, gla};
+    launch_adam_soa(reinterpret_cast<Site*>(sites), adam, g, hp, t, site_count, width, height,
+                    as_stream(stream));
+    return check_launch("sad_adam_update");
+}
+
+extern "C" sad_status_t sad_clear_gradients(float* g0, float* g1, float* g2, float* g3, float* g4,
+                                            float* g5, float* g6, float* g7, float* g8, float* g9,
+                                            uint32_t count, sad_stream_t stream) {
+    clear_error();
+    SAD_REQUIRE(count == 0 || (g0 && g1 && g2 && g3 && g4 && g5 && g6 && g7 && g8 && g9),
+                "sad_clear_gradients: null buffer");
+    if (count == 0) return SAD_OK;
+    SoaGrads g{{g0, g1, g2, g3, g4, g5, g6, g7, g8, g9}};
+    clear10_kernel<<<blocks_for(count, 256), 256, 0, as_stream(stream)>>>(g, count);
+    note_launches(1);
+    return check_launch("sad_clear_gradients");
+}
+
+extern "C" sad_status_t sad_clear_buffer(float* buffer, uint32_t count, sad_stream_t stream) {
+    clear_error();
+    SAD_REQUIRE(count == 0 || buffer, "sad_clear_buffer: null buffer");
+    launch_clear_f32(buffer, count, as_stream(stream));
+    return check_launch("sad_clear_buffer");
+}

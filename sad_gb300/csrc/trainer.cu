@@ -1,0 +1,703 @@
+// trainer.cu -- the whole fit of one image on the device.
+//
+// Iteration schedule: backends/cuda/src/sad_cuda.cu:2158-2479 (trainVoronoi).  Per
+// iteration it = 0 .. iters-1:
+//   1. every cand_update_freq iterations: f16-round the sites and run the VPT pass(es)
+//      from the current candidate field into a spare one, on a side stream (the
+//      gradient step of this iteration still reads the old field);
+//   2. on densify iterations (never at the default config, whose buffer starts full):
+//      site statistics, score, sort, split -- run eagerly, the candidate refresh then
+//      runs synchronously first, as in the reference;
+//   3. fused gradients (+ removal delta on prune iterations);
+//   4. join the side stream; 4 Jacobi passes of log-tau diffusion on the new field;
+//   5. Adam (t = it + 1) fused with the gradient clear and the refresh of the per-site
+//      records the pixel kernels gather;
+//   6. on prune iterations: score, radix sort, prune the planned count.
+//
+// Everything the host decides (which iterations refresh, densify or prune, and how
+// many sites they touch) depends only on the configuration, so the plan is computed
+// once at init and the per-iteration scalars the kernels need (Adam's t, the diffusion
+// lambda, the VPT step, the prune count) are read from device memory.  Each iteration
+// kind (refresh? prune? which candidate buffer is current?) is captured once as a CUDA
+// graph and replayed: the fit is ~4000 graph launches with no host synchronisation
+// except on log iterations.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "host_common.h"
+#include "kernels.h"
+
+namespace sad {
+
+struct IterPlan {
+    uint8_t upd, dens, prune;
+    uint32_t split_k, prune_k;
+};
+
+}  // namespace sad
+
+struct sad_trainer {
+    sad_train_config_t cfg;
+    int w = 0, h = 0, cw = 0, ch = 0, ds = 1;
+    float inv_s2 = 0.0f;
+    float prune_pct = 0.0f, densify_pct = 0.0f;
+    uint32_t cap = 0, n = 0;
+    int active = 0;
+    int iter = 0;
+    int passes = 1;
+    int cur = 0;
+    bool hilbert_ready = false;
+    uint32_t hilbert_count = 0;
+    bool have_mask = false;
+    float mask_sum = 0.0f;
+    uint32_t pow2 = 1, stages = 0;
+    std::vector<sad::IterPlan> plan;
+
+    float* target = nullptr;
+    float* mask = nullptr;
+    sad::Site* sites = nullptr;
+    sad::SiteGeom* geom = nullptr;
+    sad::SiteColor* color = nullptr;
+    sad::SiteGeom* vgeom = nullptr;
+    float* adam = nullptr;
+    float* grads = nullptr;  // [cap][12]: 10 gradients, removal delta, pad
+    float* tau_a = nullptr;
+    float* tau_b = nullptr;
+    uint32_t* pairs = nullptr;
+    void* sort_temp = nullptr;
+    uint32_t* idx = nullptr;
+    uint32_t* cand0[3] = {nullptr, nullptr, nullptr};
+    uint32_t* cand1[3] = {nullptr, nullptr, nullptr};
+    uint32_t* horder = nullptr;
+    uint32_t* hpos = nullptr;
+    uint32_t* hpairs = nullptr;
+    uint32_t hpadded = 0;
+    float* stats = nullptr;  // 8 x cap
+    float* render = nullptr;
+    float* metric = nullptr;
+    uint32_t* count = nullptr;
+    sad::DevState* state = nullptr;
+    uint32_t* prune_k = nullptr;
+    void* init_temp = nullptr;
+    std::vector<void*> allocs;
+
+    cudaStream_t st = nullptr, side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaGraphExec_t graphs[2][2][3] = {};
+    bool timing = false;
+    std::vector<cudaEvent_t> tev;
+    size_t tev_used = 0;
+    double grad_ms = 0.0;
+    int grad_launches = 0;
+    std::chrono::steady_clock::time_point t0;
+};
+
+namespace sad {
+
+static sad_status_t dalloc(sad_trainer* t, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        set_error("trainer allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? SAD_ERR_OUT_OF_MEMORY : SAD_ERR_CUDA;
+    }
+    t->allocs.push_back(*p);
+    return SAD_OK;
+}
+
+template <class T>
+static sad_status_t dalloc_n(sad_trainer* t, T** p, size_t count) {
+    return dalloc(t, reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+static void drop_graphs(sad_trainer* t) {
+    for (auto& a : t->graphs)
+        for (auto& b : a)
+            for (auto& g : b)
+                if (g) {
+                    cudaGraphExecDestroy(g);
+                    g = nullptr;
+                }
+}
+
+// Host plan of the whole schedule (the same decisions the reference makes at run time).
+static void make_plan(sad_trainer* t) {
+    const sad_train_config_t& c = t->cfg;
+    t->plan.assign(std::max(0, c.iterations), IterPlan{});
+    int eff_prune_start = c.prune_start;
+    if (c.densify && !c.prune_during_densify && c.prune_start < c.densify_end)
+        eff_prune_start = c.densify_end;
+    int eff_prune_end = c.prune_end > 0 ? c.prune_end : c.iterations - 1;
+    int active = t->active;
+    uint32_t n = t->n;
+    for (int it = 0; it < c.iterations; ++it) {
+        IterPlan& p = t->plan[it];
+        p.upd = c.cand_update_freq > 0 && it % c.cand_update_freq == 0;
+        int desired = std::max(0, static_cast<int>(active * t->densify_pct));
+        bool dens = c.densify && it >= c.densify_start && it <= c.densify_end &&
+                    it % std::max(1, c.densify_freq) == 0 && n < t->cap && desired > 0;
+        if (dens) {
+            int avail = static_cast<int>(t->cap - n);
+            int k = std::min(desired, std::min(avail, SAD_MAX_SPLIT_INDICES));
+            if (k > 0) {
+                p.dens = 1;
+                p.split_k = static_cast<uint32_t>(k);
+                n += k;
+                active += k;
+            }
+        }
+        bool prune = t->prune_pct > 0.0f && it >= eff_prune_start && it < eff_prune_end &&
+                     it % std::max(1, c.prune_freq) == 0;
+        if (prune) {
+            p.prune = 1;
+            int k = std::min(std::max(0, static_cast<int>(active * t->prune_pct)), SAD_MAX_SPLIT_INDICES);
+            p.prune_k = static_cast<uint32_t>(k);
+            active = std::max(0, active - k);
+        }
+    }
+}
+
+static sad_status_t build_hilbert(sad_trainer* t, cudaStream_t s) {
+    int bits = sad_hilbert_bits_for_size(t->w, t->h);
+    uint32_t padded = (t->n + 1023u) / 1024u * 1024u;
+    padded = std::min(padded, std::max(1u, t->hpadded));
+    launch_hilbert_pairs(t->sites, t->hpairs, t->n, padded, t->w, t->h, bits, s);
+    uint32_t maxk = bits >= 16 ? 0xFFFFFFFFu : (1u << (2 * bits));
+    launch_radix_sort(t->hpairs, padded, maxk, t->sort_temp, s);
+    launch_hilbert_order(t->hpairs, t->horder, t->hpos, t->n, s);
+    t->hilbert_ready = true;
+    t->hilbert_count = t->n;
+    return check_launch("trainer hilbert order");
+}
+
+static VptParams vpt_params(sad_trainer* t) {
+    VptParams p{};
+    const sad_train_config_t& c = t->cfg;
+    bool use_h = c.cand_hilbert_probes > 0 && c.cand_hilbert_window > 0;
+    p.site_count = t->n;
+    p.inv_scale_sq = t->inv_s2;
+    p.radius_scale = c.cand_radius_scale;
+    p.radius_probes = c.cand_radius_probes;
+    p.inject_count = t->n == 0 ? 0u : c.cand_inject_count;
+    p.hilbert_order = use_h ? t->horder : nullptr;
+    p.hilbert_pos = use_h ? t->hpos : nullptr;
+    p.hilbert_probes = use_h ? c.cand_hilbert_probes : 0u;
+    p.hilbert_window = use_h ? c.cand_hilbert_window : 0u;
+    p.cand_downscale = t->ds;
+    p.target_width = t->w;
+    p.target_height = t->h;
+    p.width = t->cw;
+    p.height = t->ch;
+    p.state = t->state;
+    p.pow2 = t->pow2;
+    p.stages = t->stages;
+    return p;
+}
+
+// VPT passes from field `src` into the spare fields; returns the final field index.
+static int launch_refresh(sad_trainer* t, int src, cudaStream_t s) {
+    launch_pack_geom(t->sites, t->vgeom, t->n, s);
+    int o[2], k = 0;
+    for (int b = 0; b < 3; ++b)
+        if (b != src) o[k++] = b;
+    VptParams p = vpt_params(t);
+    int in = src;
+    for (int pass = 0; pass < t->passes; ++pass) {
+        int out = o[pass & 1];
+        p.in0 = t->cand0[in];
+        p.in1 = t->cand1[in];
+        p.out0 = t->cand0[out];
+        p.out1 = t->cand1[out];
+        p.pass_offset = static_cast<uint32_t>(pass);
+        launch_vpt_geom(p, t->vgeom, s);
+        in = out;
+    }
+    return in;
+}
+
+static int refresh_target(sad_trainer* t, int src) {
+    int o[2], k = 0;
+    for (int b = 0; b < 3; ++b)
+        if (b != src) o[k++] = b;
+    return o[(t->passes - 1) & 1];
+}
+
+static void launch_gradients_step(sad_trainer* t, int field, bool prune, cudaStream_t s) {
+    GradParams g{};
+    g.cand0 = t->cand0[field];
+    g.cand1 = t->cand1[field];
+    g.target = t->target;
+    g.rendered = t->render;
+    g.mask = t->have_mask ? t->mask : nullptr;
+    g.inv_scale_sq = t->inv_s2;
+    g.site_count = t->n;
+    g.ssim_weight = t->cfg.ssim_weight;
+    g.width = t->w;
+    g.height = t->h;
+    g.cand_width = t->cw;
+    g.cand_height = t->ch;
+    g.aos12 = t->grads;
+    g.compute_removal = prune ? 1 : 0;
+    launch_gradients_prepared(g, t->geom, t->color, s);
+}
+
+// Steps 3-6 of one iteration (and the fork/join of step 1 when `upd`), then the counter
+// advance.  `field` is the current candidate field; returns the field current after it.
+static int iteration_body(sad_trainer* t, bool upd, bool prune, int field, int adv_passes,
+                          cudaStream_t s) {
+    int next = field;
+    if (upd) {
+        cudaEventRecord(t->ev_fork, s);
+        cudaStreamWaitEvent(t->side, t->ev_fork, 0);
+        next = launch_refresh(t, field, t->side);
+        cudaEventRecord(t->ev_join, t->side);
+    }
+    if (t->cfg.ssim_weight > 0.0f)
+        launch_render_prepared(t->cand0[field], t->cand1[field], t->render, t->geom, t->color,
+                               t->inv_s2, t->n, t->w, t->h, t->cw, t->ch, s);
+    bool timed = t->timing && t->tev_used + 2 <= t->tev.size();
+    if (timed) cudaEventRecord(t->tev[t->tev_used], s);
+    launch_gradients_step(t, field, prune, s);
+    if (timed) {
+        cudaEventRecord(t->tev[t->tev_used + 1], s);
+        t->tev_used += 2;
+    }
+    if (upd) cudaStreamWaitEvent(s, t->ev_join, 0);
+    // 4 Jacobi passes: grads slot 2 -> A -> B -> A -> B
+    const float* gin = t->grads + 2;
+    int stride = 12;
+    float* bufs[2] = {t->tau_a, t->tau_b};
+    for (int pass = 0; pass < 4; ++pass) {
+        float* out = bufs[pass & 1];
+        launch_tau_diffuse_train(t->cand0[next], t->cand1[next], t->geom, t->grads, gin, stride,
+                                 out, t->n, t->state, t->cfg.iterations, t->cw, t->ch, t->ds, s);
+        gin = out;
+        stride = 1;
+    }
+    AdamHyper hp{t->cfg.lr_pos * t->cfg.lr_scale, t->cfg.lr_tau * t->cfg.lr_scale,
+                 t->cfg.lr_radius * t->cfg.lr_scale, t->cfg.lr_color * t->cfg.lr_scale,
+                 t->cfg.lr_dir * t->cfg.lr_scale, t->cfg.lr_aniso * t->cfg.lr_scale,
+                 t->cfg.beta1, t->cfg.beta2, t->cfg.eps};
+    launch_adam_train(t->sites, t->adam, t->grads, t->tau_b, t->geom, t->color, hp, t->state,
+                      t->n, t->w, t->h, s);
+    if (prune) {
+        float delta_norm = 1.0f / std::max(1.0f, t->mask_sum);
+        launch_prune_pairs(t->sites, t->grads + 10, 12, t->pairs, t->n, delta_norm, t->cap, s);
+        launch_radix_sort(t->pairs, t->cap, 0xFFFFFFFFu, t->sort_temp, s);
+        launch_prune_sorted_train(t->sites, t->geom, t->pairs, t->prune_k, t->state,
+                                  SAD_MAX_SPLIT_INDICES, s);
+    }
+    launch_advance_state(t->state, static_cast<uint32_t>(adv_passes), s);
+    return next;
+}
+
+static sad_status_t run_densify(sad_trainer* t, const IterPlan& p, cudaStream_t s) {
+    // site statistics on the current field, score, sort, split (sad_cuda.cu:2232-2292)
+    float* st[8];
+    for (int k = 0; k < 8; ++k) st[k] = t->stats + static_cast<size_t>(k) * t->cap;
+    launch_clear_f32(t->stats, static_cast<size_t>(8) * t->cap, s);
+    launch_site_stats(t->cand0[t->cur], t->cand1[t->cur], t->target,
+                      t->have_mask ? t->mask : nullptr, t->sites, t->inv_s2, t->n, st, t->w, t->h,
+                      t->cw, t->ch, s);
+    launch_densify_pairs(t->sites, st[0], st[1], t->pairs, t->n, 1.0f, t->cfg.densify_score_alpha,
+                         t->cap, s);
+    launch_radix_sort(t->pairs, t->cap, 0xFFFFFFFFu, t->sort_temp, s);
+    launch_write_indices(t->pairs, t->idx, p.split_k, s);
+    const float* sp[7] = {st[0], st[2], st[3], st[4], st[5], st[6], st[7]};
+    launch_split(t->sites, t->adam, t->idx, p.split_k, sp, t->n, t->target, t->w, t->h, s);
+    t->n += p.split_k;
+    t->active += static_cast<int>(p.split_k);
+    launch_prepare_sites(t->sites, t->geom, t->color, t->n, s);
+    drop_graphs(t);  // site count changed
+    return check_launch("trainer densify");
+}
+
+static sad_status_t capture_variant(sad_trainer* t, bool upd, bool prune, int field,
+                                    cudaGraphExec_t* out) {
+    cudaGraph_t graph = nullptr;
+    SAD_TRY(check_cuda(cudaStreamBeginCapture(t->st, cudaStreamCaptureModeThreadLocal),
+                       "trainer graph capture"));
+    iteration_body(t, upd, prune, field, upd ? t->passes : 0, t->st);
+    cudaError_t e = cudaStreamEndCapture(t->st, &graph);
+    if (e != cudaSuccess) return check_cuda(e, "trainer graph capture end");
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    return check_cuda(e, "trainer graph instantiate");
+}
+
+static sad_status_t log_iteration(sad_trainer* t, int it) {
+    float psnr = 0.0f;
+    SAD_TRY(sad_trainer_render(t, nullptr, &psnr));
+    uint32_t active = 0;
+    SAD_TRY(check_cuda(cudaMemsetAsync(t->count, 0, 4, t->st), "trainer count"));
+    launch_count_active(t->sites, t->count, t->n, t->st);
+    SAD_TRY(check_cuda(cudaMemcpyAsync(&active, t->count, 4, cudaMemcpyDeviceToHost, t->st),
+                       "trainer count copy"));
+    SAD_TRY(check_cuda(cudaStreamSynchronize(t->st), "trainer log sync"));
+    double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t->t0).count();
+    double its = el > 0 ? (it + 1) / el : 0.0;
+    printf("Iter %4d | PSNR: %.2f dB | Active: %u/%u | %.1f it/s | %.1fs\n", it, psnr, active, t->n,
+           its, el);
+    fflush(stdout);
+    return SAD_OK;
+}
+
+}  // namespace sad
+
+using namespace sad;
+
+extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int width, int height,
+                                           sad_trainer_t** out) {
+    clear_error();
+    SAD_REQUIRE(cfg && out, "sad_trainer_create: null argument");
+    SAD_REQUIRE(width > 0 && height > 0, "sad_trainer_create: invalid image size");
+    SAD_REQUIRE(cfg->iterations >= 0, "sad_trainer_create: negative iterations");
+    SAD_REQUIRE(cfg->n_sites > 0, "sad_trainer_create: n_sites must be positive");
+    SAD_REQUIRE(cfg->cand_update_passes >= 0, "sad_trainer_create: negative candidate passes");
+    sad_trainer* t = new sad_trainer();
+    *out = nullptr;
+    t->cfg = *cfg;
+    t->w = width;
+    t->h = height;
+    t->ds = std::max(1, cfg->cand_downscale);
+    t->cw = std::max(1, (width + t->ds - 1) / t->ds);
+    t->ch = std::max(1, (height + t->ds - 1) / t->ds);
+    float md = static_cast<float>(std::max(width, height));
+    t->inv_s2 = 1.0f / (md * md);
+    t->passes = std::max(1, cfg->cand_update_passes);
+    jump_schedule_constants(t->cw, t->ch, &t->pow2, &t->stages);
+    int num_pixels = width * height;
+    // planSiteCapacity (sad_cuda.cu:1079-1101)
+    int max_cap = cfg->max_sites > 0 ? cfg->max_sites
+                  : cfg->densify  ? std::min(num_pixels * 2, std::max(cfg->n_sites * 8, 8192))
+                                  : num_pixels * 2;
+    int requested = cfg->densify ? max_cap : cfg->n_sites;
+    t->cap = static_cast<uint32_t>(std::max(cfg->n_sites, requested));
+    t->prune_pct = cfg->prune_percentile;
+    t->densify_pct = cfg->densify_percentile;
+    if (cfg->target_bpp > 0.0f) {
+        int prune_end = cfg->prune_end > 0 ? cfg->prune_end : cfg->iterations - 1;
+        sad_bpp_solution_t sol{};
+        sad_status_t s = sad_solve_target_bpp(
+            cfg->target_bpp, width, height, cfg->n_sites, max_cap, cfg->iterations, cfg->densify,
+            cfg->densify_start, cfg->densify_end, std::max(1, cfg->densify_freq),
+            cfg->densify_percentile, cfg->prune_during_densify, cfg->prune_start, prune_end,
+            std::max(1, cfg->prune_freq), cfg->prune_percentile, SAD_MAX_SPLIT_INDICES, &sol);
+        if (s != SAD_OK) {
+            delete t;
+            return s;
+        }
+        t->densify_pct = sol.densify_percentile;
+        t->prune_pct = sol.prune_percentile;
+    }
+    size_t np = static_cast<size_t>(width) * height;
+    size_t nc = static_cast<size_t>(t->cw) * t->ch * 4;
+    uint32_t cap = t->cap;
+    t->hpadded = (cap + 1023u) / 1024u * 1024u;
+    size_t sort_bytes = radix_sort_temp_bytes(std::max(cap, t->hpadded));
+    sad_status_t s = SAD_OK;
+#define ALLOC(p, cnt)                                  \
+    if (s == SAD_OK) s = dalloc_n(t, &(p), (cnt));
+    ALLOC(t->target, np * 3);
+    ALLOC(t->mask, np);
+    ALLOC(t->sites, cap);
+    ALLOC(t->geom, cap);
+    ALLOC(t->color, cap);
+    ALLOC(t->vgeom, cap);
+    ALLOC(t->adam, static_cast<size_t>(cap) * 20);
+    ALLOC(t->grads, static_cast<size_t>(cap) * 12);
+    ALLOC(t->tau_a, cap);
+    ALLOC(t->tau_b, cap);
+    ALLOC(t->pairs, static_cast<size_t>(cap) * 2);
+    ALLOC(t->idx, SAD_MAX_SPLIT_INDICES);
+    for (int b = 0; b < 3; ++b) {
+        ALLOC(t->cand0[b], nc);
+        ALLOC(t->cand1[b], nc);
+    }
+    ALLOC(t->horder, cap);
+    ALLOC(t->hpos, cap);
+    ALLOC(t->hpairs, static_cast<size_t>(t->hpadded) * 2);
+    ALLOC(t->stats, static_cast<size_t>(cap) * 8);
+    ALLOC(t->render, np * 3);
+    ALLOC(t->metric, 4);
+    ALLOC(t->count, 4);
+    ALLOC(t->state, 1);
+    ALLOC(t->prune_k, std::max(1, cfg->iterations));
+#undef ALLOC
+    if (s == SAD_OK) s = dalloc(t, &t->sort_temp, sort_bytes);
+    if (s == SAD_OK) s = dalloc(t, &t->init_temp, init_temp_bytes(static_cast<uint32_t>(cfg->n_sites)));
+    if (s == SAD_OK)
+        s = check_cuda(cudaStreamCreateWithFlags(&t->st, cudaStreamNonBlocking), "trainer stream");
+    if (s == SAD_OK)
+        s = check_cuda(cudaStreamCreateWithFlags(&t->side, cudaStreamNonBlocking), "trainer stream");
+    if (s == SAD_OK)
+        s = check_cuda(cudaEventCreateWithFlags(&t->ev_fork, cudaEventDisableTiming), "trainer event");
+    if (s == SAD_OK)
+        s = check_cuda(cudaEventCreateWithFlags(&t->ev_join, cudaEventDisableTiming), "trainer event");
+    if (s != SAD_OK) {
+        std::string msg = sad_last_error();
+        sad_trainer_destroy(t);
+        set_error("%s", msg.c_str());
+        return s;
+    }
+    // all-ones mask until a target is given
+    *out = t;
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_trainer_destroy(sad_trainer_t* t) {
+    if (!t) return SAD_OK;
+    if (t->st) cudaStreamSynchronize(t->st);
+    if (t->side) cudaStreamSynchronize(t->side);
+    drop_graphs(t);
+    for (cudaEvent_t e : t->tev) cudaEventDestroy(e);
+    if (t->ev_fork) cudaEventDestroy(t->ev_fork);
+    if (t->ev_join) cudaEventDestroy(t->ev_join);
+    if (t->st) cudaStreamDestroy(t->st);
+    if (t->side) cudaStreamDestroy(t->side);
+    for (void* p : t->allocs) cudaFree(p);
+    delete t;
+    return SAD_OK;
+}
+
+extern "C" sad_stream_t sad_trainer_stream(sad_trainer_t* t) {
+    return t ? reinterpret_cast<sad_stream_t>(t->st) : nullptr;
+}
+
+static sad_status_t set_mask_common(sad_trainer* t, bool have_mask) {
+    t->have_mask = have_mask;
+    if (!have_mask) {
+        t->mask_sum = static_cast<float>(static_cast<size_t>(t->w) * t->h);
+        return SAD_OK;
+    }
+    // the mask sum normalises the removal delta and the PSNR (read back once per target)
+    std::vector<float> host(static_cast<size_t>(t->w) * t->h);
+    SAD_TRY(check_cuda(cudaMemcpyAsync(host.data(), t->mask, host.size() * 4, cudaMemcpyDeviceToHost, t->st),
+                       "trainer mask readback"));
+    SAD_TRY(check_cuda(cudaStreamSynchronize(t->st), "trainer mask sync"));
+    double sum = 0.0;
+    for (float v : host) sum += v;
+    t->mask_sum = static_cast<float>(sum);
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_trainer_set_target_device(sad_trainer_t* t, const float* target,
+                                                      const float* mask) {
+    clear_error();
+    SAD_REQUIRE(t && target, "sad_trainer_set_target_device: null argument");
+    size_t np = static_cast<size_t>(t->w) * t->h;
+    SAD_TRY(check_cuda(cudaMemcpyAsync(t->target, target, np * 12, cudaMemcpyDeviceToDevice, t->st),
+                       "trainer target copy"));
+    if (mask)
+        SAD_TRY(check_cuda(cudaMemcpyAsync(t->mask, mask, np * 4, cudaMemcpyDeviceToDevice, t->st),
+                           "trainer mask copy"));
+    return set_mask_common(t, mask != nullptr);
+}
+
+extern "C" sad_status_t sad_trainer_set_target_host(sad_trainer_t* t, const float* target_host,
+                                                    const float* mask_host) {
+    clear_error();
+    SAD_REQUIRE(t && target_host, "sad_trainer_set_target_host: null argument");
+    size_t np = static_cast<size_t>(t->w) * t->h;
+    SAD_TRY(check_cuda(cudaMemcpyAsync(t->target, target_host, np * 12, cudaMemcpyHostToDevice, t->st),
+                       "trainer target upload"));
+    if (mask_host)
+        SAD_TRY(check_cuda(cudaMemcpyAsync(t->mask, mask_host, np * 4, cudaMemcpyHostToDevice, t->st),
+                           "trainer mask upload"));
+    return set_mask_common(t, mask_host != nullptr);
+}
+
+__global__ void fill_inactive_kernel(sad::Site* sites, uint32_t from, uint32_t to) {
+    uint32_t i = from + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= to) return;
+    sad::Site s{};
+    s.px = -1.0f;
+    s.py = -1.0f;
+    s.dx = 1.0f;
+    sites[i] = s;
+}
+
+extern "C" sad_status_t sad_trainer_init(sad_trainer_t* t, const float* sites_host, int n) {
+    clear_error();
+    SAD_REQUIRE(t, "sad_trainer_init: null trainer");
+    cudaStream_t s = t->st;
+    uint32_t n0;
+    int active;
+    if (sites_host) {
+        SAD_REQUIRE(n > 0 && static_cast<uint32_t>(n) <= t->cap, "sad_trainer_init: site count exceeds capacity");
+        n0 = static_cast<uint32_t>(n);
+        SAD_TRY(check_cuda(cudaMemcpyAsync(t->sites, sites_host, static_cast<size_t>(n) * 40,
+                                           cudaMemcpyHostToDevice, s),
+                           "trainer sites upload"));
+        active = 0;
+        for (int i = 0; i < n; ++i) active += sites_host[static_cast<size_t>(i) * 10] >= 0.0f;
+    } else {
+        n0 = static_cast<uint32_t>(t->cfg.n_sites);
+        SAD_REQUIRE(n0 <= t->cap, "sad_trainer_init: n_sites exceeds capacity");
+        float thr = 0.01f * t->cfg.init_gradient_alpha;
+        SAD_TRY(check_cuda(run_init_gradient_weighted(t->sites, n0, t->target,
+                                                      t->have_mask ? t->mask : nullptr, thr, 256,
+                                                      t->cfg.init_log_tau, t->cfg.init_radius,
+                                                      t->w, t->h, t->init_temp, s),
+                           "trainer gradient-weighted init"));
+        active = static_cast<int>(n0);  // the reference counts its (zeroed) host sites here
+    }
+    if (n0 < t->cap) {
+        fill_inactive_kernel<<<blocks_for(t->cap - n0, 256), 256, 0, s>>>(t->sites, n0, t->cap);
+        note_launches(1);
+    }
+    launch_prepare_sites(t->sites, t->geom, t->color, t->cap, s);
+    SAD_TRY(check_cuda(cudaMemsetAsync(t->adam, 0, static_cast<size_t>(t->cap) * 80, s), "trainer adam clear"));
+    SAD_TRY(check_cuda(cudaMemsetAsync(t->grads, 0, static_cast<size_t>(t->cap) * 48, s), "trainer grad clear"));
+    SAD_TRY(check_cuda(cudaMemsetAsync(t->state, 0, sizeof(DevState), s), "trainer state clear"));
+    t->n = n0;
+    t->active = active;
+    t->iter = 0;
+    t->cur = 0;
+    t->hilbert_ready = false;
+    launch_init_candidates(t->cand0[0], t->cand1[0], n0, 0u, 0, t->cw, t->ch, s);
+    launch_jfa_seed(t->cand0[0], t->sites, n0, t->cw, t->ch, t->ds, s);
+    make_plan(t);
+    std::vector<uint32_t> pk(std::max(1, t->cfg.iterations), 0u);
+    for (size_t i = 0; i < t->plan.size(); ++i) pk[i] = t->plan[i].prune_k;
+    SAD_TRY(check_cuda(cudaMemcpyAsync(t->prune_k, pk.data(), pk.size() * 4, cudaMemcpyHostToDevice, s),
+                       "trainer plan upload"));
+    SAD_TRY(check_cuda(cudaStreamSynchronize(s), "trainer init sync"));
+    drop_graphs(t);
+    t->grad_ms = 0.0;
+    t->grad_launches = 0;
+    t->t0 = std::chrono::steady_clock::now();
+    return check_launch("sad_trainer_init");
+}
+
+extern "C" sad_status_t sad_trainer_enable_timing(sad_trainer_t* t, int enable) {
+    clear_error();
+    SAD_REQUIRE(t, "sad_trainer_enable_timing: null trainer");
+    t->timing = enable != 0;
+    if (t->timing && t->tev.empty()) {
+        t->tev.resize(2 * static_cast<size_t>(std::max(1, t->cfg.iterations)));
+        for (auto& e : t->tev) SAD_TRY(check_cuda(cudaEventCreate(&e), "trainer timing events"));
+    }
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_trainer_run(sad_trainer_t* t, int end) {
+    clear_error();
+    SAD_REQUIRE(t, "sad_trainer_run: null trainer");
+    SAD_REQUIRE(end >= t->iter && end <= t->cfg.iterations, "sad_trainer_run: end out of range");
+    const sad_train_config_t& c = t->cfg;
+    bool use_h = c.cand_hilbert_probes > 0 && c.cand_hilbert_window > 0;
+    bool eager = !c.use_graphs || t->timing;
+    t->tev_used = 0;
+    for (int it = t->iter; it < end; ++it) {
+        const IterPlan& p = t->plan[it];
+        if (p.upd && use_h && (!t->hilbert_ready || t->hilbert_count != t->n))
+            SAD_TRY(build_hilbert(t, t->st));
+        if (p.dens) {
+            bool upd = p.upd;
+            if (upd) t->cur = launch_refresh(t, t->cur, t->st);  // synchronous refresh
+            SAD_TRY(run_densify(t, p, t->st));
+            t->cur = iteration_body(t, false, p.prune, t->cur, upd ? t->passes : 0, t->st);
+        } else if (eager) {
+            t->cur = iteration_body(t, p.upd, p.prune, t->cur, p.upd ? t->passes : 0, t->st);
+        } else {
+            cudaGraphExec_t& g = t->graphs[p.upd][p.prune][t->cur];
+            if (!g) SAD_TRY(capture_variant(t, p.upd, p.prune, t->cur, &g));
+            SAD_TRY(check_cuda(cudaGraphLaunch(g, t->st), "trainer graph launch"));
+            note_launches(p.upd ? (1 + t->passes + 7 + (p.prune ? 9 : 0))
+                                : (7 + (p.prune ? 9 : 0)));
+            if (p.upd) t->cur = refresh_target(t, t->cur);
+        }
+        SAD_TRY(check_launch("sad_trainer_run"));
+        t->iter = it + 1;
+        if (c.log_freq > 0 && (it % c.log_freq == 0 || it == c.iterations - 1))
+            SAD_TRY(log_iteration(t, it));
+    }
+    if (t->timing && t->tev_used > 0) {
+        SAD_TRY(check_cuda(cudaStreamSynchronize(t->st), "trainer timing sync"));
+        for (size_t i = 0; i + 1 < t->tev_used; i += 2) {
+            float ms = 0.0f;
+            SAD_TRY(check_cuda(cudaEventElapsedTime(&ms, t->tev[i], t->tev[i + 1]), "trainer timing"));
+            t->grad_ms += ms;
+            t->grad_launches += 1;
+        }
+    }
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_trainer_render(sad_trainer_t* t, float* rgb_out, float* psnr_out) {
+    clear_error();
+    SAD_REQUIRE(t, "sad_trainer_render: null trainer");
+    launch_render_prepared(t->cand0[t->cur], t->cand1[t->cur], t->render, t->geom, t->color,
+                           t->inv_s2, t->n, t->w, t->h, t->cw, t->ch, t->st);
+    if (rgb_out)
+        SAD_TRY(check_cuda(cudaMemcpyAsync(rgb_out, t->render, static_cast<size_t>(t->w) * t->h * 12,
+                                           cudaMemcpyDeviceToDevice, t->st),
+                           "trainer render copy"));
+    if (psnr_out) {
+        float sum = 0.0f;
+        SAD_TRY(check_cuda(cudaMemsetAsync(t->metric, 0, 4, t->st), "trainer metric clear"));
+        launch_mse(t->render, t->target, t->have_mask ? t->mask : nullptr, t->metric, t->w, t->h, t->st);
+        SAD_TRY(check_cuda(cudaMemcpyAsync(&sum, t->metric, 4, cudaMemcpyDeviceToHost, t->st),
+                           "trainer metric copy"));
+        SAD_TRY(check_cuda(cudaStreamSynchronize(t->st), "trainer render sync"));
+        float mse = sum / (std::max(1.0f, t->mask_sum) * 3.0f);
+        *psnr_out = mse > 0.0f ? 20.0f * log10f(1.0f / sqrtf(mse)) : 100.0f;
+    }
+    return check_launch("sad_trainer_render");
+}
+
+extern "C" sad_status_t sad_trainer_get_sites(sad_trainer_t* t, float* sites_host, int capacity,
+                                              int active_only, int* written) {
+    clear_error();
+    SAD_REQUIRE(t && sites_host && written, "sad_trainer_get_sites: null argument");
+    std::vector<float> all(static_cast<size_t>(t->n) * 10);
+    SAD_TRY(check_cuda(cudaMemcpyAsync(all.data(), t->sites, all.size() * 4, cudaMemcpyDeviceToHost, t->st),
+                       "trainer sites download"));
+    SAD_TRY(check_cuda(cudaStreamSynchronize(t->st), "trainer sites sync"));
+    int k = 0;
+    for (uint32_t i = 0; i < t->n && k < capacity; ++i) {
+        const float* s = all.data() + static_cast<size_t>(i) * 10;
+        if (active_only && !(s[0] >= 0.0f)) continue;
+        std::memcpy(sites_host + static_cast<size_t>(k) * 10, s, 40);
+        ++k;
+    }
+    *written = k;
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_trainer_info(sad_trainer_t* t, sad_trainer_info_t* info) {
+    clear_error();
+    SAD_REQUIRE(t && info, "sad_trainer_info: null argument");
+    info->width = t->w;
+    info->height = t->h;
+    info->iteration = t->iter;
+    info->site_buffer = static_cast<int>(t->n);
+    info->active_estimate = t->active;
+    info->capacity = static_cast<int>(t->cap);
+    info->prune_percentile = t->prune_pct;
+    info->densify_percentile = t->densify_pct;
+    info->gpu_ms_gradients = t->grad_ms;
+    info->gradient_launches = t->grad_launches;
+    info->kernel_launches = sad_launch_count();
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_trainer_fit_host(sad_trainer_t* t, const float* target_host,
+                                             const float* mask_host, float* sites_host,
+                                             int capacity, int* written, float* psnr_out) {
+    clear_error();
+    SAD_REQUIRE(t && target_host, "sad_trainer_fit_host: null argument");
+    SAD_TRY(sad_trainer_set_target_host(t, target_host, mask_host));
+    SAD_TRY(sad_trainer_init(t, nullptr, 0));
+    SAD_TRY(sad_trainer_run(t, t->cfg.iterations));
+    SAD_TRY(sad_trainer_render(t, nullptr, psnr_out));
+    if (sites_host) {
+        SAD_REQUIRE(written, "sad_trainer_fit_host: null written");
+        SAD_TRY(sad_trainer_get_sites(t, sites_host, capacity, 1, written));
+    }
+    return SAD_OK;
+}

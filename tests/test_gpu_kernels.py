@@ -1,0 +1,449 @@
+"""Parity of every sm_103a kernel with the CPU oracle, called through the C ABI (via the
+torch.ops.sad-compatible op layer), on seeded inputs that include the edge cases the
+reference handles: empty slots, out-of-range ids, inactive sites, duplicated ids, ragged
+sizes and padded candidate fields.
+
+Tolerances (stated here, used below):
+  * integer / index work (candidate init, seeds, packing, sort, Hilbert order, prune
+    selection, init positions): bit-exact;
+  * candidate lists from distance ranking: identical except where two distances agree to
+    1e-5 relative (CPU libm expf / no-FMA vs CUDA), and identical lists on >= 99% pixels;
+  * rendered RGB: max abs error <= 1e-4;
+  * per-site gradients: |gpu - oracle| <= 1e-3 * (sum over pixels of |term|) + 1e-6 per
+    component (the oracle sums in double; the GPU's float atomics have no fixed order).
+"""
+import numpy as np
+import pytest
+import torch
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+U32 = 0xFFFFFFFF
+
+
+def t32(a):
+    """uint32 / int32 numpy -> int32 CUDA tensor with the same bits."""
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).cuda()
+
+
+def tf(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+
+
+def u32(t):
+    return t.cpu().numpy().view(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def ops(cuda):
+    from sad_gb300 import ops as _ops
+    return _ops
+
+
+def packed_dist_np(sites, ids, xs, ys, inv_s2):
+    """Candidate distance of the VPT pass from f16-rounded site values (float64)."""
+    s = sites.astype(np.float16).astype(np.float64)
+    ok = ids < sites.shape[0]
+    i = np.where(ok, ids, 0)
+    g = s[i]
+    dx, dy = xs - g[..., 0], ys - g[..., 1]
+    proj = g[..., 7] * dx + g[..., 8] * dy
+    perp2 = np.maximum(dx * dx + dy * dy - proj * proj, 0)
+    l1 = np.exp(g[..., 9])
+    d2 = np.maximum((l1 * proj * proj + perp2 / l1) * inv_s2, 1e-8)
+    d = np.maximum(np.exp(g[..., 2]), 1e-4) * (np.sqrt(d2) - g[..., 3] * np.sqrt(inv_s2))
+    d = np.where(g[..., 0] < 0, np.inf, d)
+    return np.where(ok, d, np.inf)
+
+
+def raw_dist_np(sites, ids, xs, ys, inv_s2):
+    s = sites.astype(np.float64)
+    ok = ids < sites.shape[0]
+    g = s[np.where(ok, ids, 0)]
+    dx, dy = xs - g[..., 0], ys - g[..., 1]
+    proj = g[..., 7] * dx + g[..., 8] * dy
+    perp2 = np.maximum(dx * dx + dy * dy - proj * proj, 0)
+    l1 = np.exp(g[..., 9])
+    d2 = np.maximum((l1 * proj * proj + perp2 / l1) * inv_s2, 1e-8)
+    d = np.maximum(np.exp(g[..., 2]), 1e-4) * (np.sqrt(d2) - g[..., 3] * np.sqrt(inv_s2))
+    d = np.where(g[..., 0] < 0, np.inf, d)
+    return np.where(ok, d, np.inf)
+
+
+def assert_lists_match(got, want, dist_fn, w, h, min_exact=0.99):
+    """Tie-tolerant list comparison: lists may differ only where distances tie."""
+    got, want = got.reshape(w * h, -1), want.reshape(w * h, -1)
+    same = np.all(got == want, axis=1)
+    assert same.mean() >= min_exact, same.mean()
+    bad = np.nonzero(~same)[0]
+    if bad.size:
+        xs = (bad % w)[:, None].astype(np.float64)
+        ys = (bad // w)[:, None].astype(np.float64)
+        dg = np.sort(dist_fn(got[bad], xs, ys), axis=1)
+        dw = np.sort(dist_fn(want[bad], xs, ys), axis=1)
+        fin = np.isfinite(dg) & np.isfinite(dw)
+        assert np.array_equal(np.isfinite(dg), np.isfinite(dw))
+        assert np.all(np.abs(dg[fin] - dw[fin]) <= 1e-5 * np.maximum(np.abs(dw[fin]), 1e-3))
+
+
+# ---------------------------------------------------------------------------
+# render and adjoint
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("w,h,n,seed", [(61, 37, 300, 1), (256, 256, 4096, 2), (128, 96, 40, 3)])
+def test_render_matches_oracle(ops, orc, w, h, n, seed):
+    img, sites = cases.scene(w, h, n, seed)
+    sites[::13, 0] = -1.0
+    c0, c1 = cases.random_field(w, h, n, seed)
+    got = ops.render_sad(t32(c0), t32(c1), tf(sites), 1.0 / max(w, h) ** 2, w, h).cpu().numpy()
+    want = orc.render(c0, c1, sites, w, h)
+    assert np.max(np.abs(got - want)) <= 1e-4
+
+
+def test_render_padded_candidate_field(ops, orc):
+    w, h, cw, ch, n = 100, 70, 50, 35, 500
+    img, sites = cases.scene(w, h, n, 4)
+    c0, c1 = cases.random_field(cw, ch, n, 4)
+    got = ops.render_sad_padded(t32(c0), t32(c1), tf(sites), 1.0 / w ** 2, w, h, cw, ch).cpu().numpy()
+    want = orc.render(c0, c1, sites, w, h, cw, ch)
+    assert np.max(np.abs(got - want)) <= 1e-4
+
+
+def test_render_all_invalid_black(ops):
+    w, h, n = 33, 9, 5
+    sites = np.zeros((n, 10), np.float32)
+    sites[:, 0] = -1
+    c0 = np.full((w * h, 4), U32, np.uint32)
+    c1 = np.full((w * h, 4), n + 3, np.uint32)
+    out = ops.render_sad(t32(c0), t32(c1), tf(sites), 1e-3, w, h)
+    assert torch.count_nonzero(out).item() == 0
+
+
+@pytest.mark.parametrize("w,h,n,seed", [(64, 48, 256, 5), (200, 130, 3000, 6)])
+def test_render_backward_matches_oracle(ops, orc, w, h, n, seed):
+    img, sites = cases.scene(w, h, n, seed)
+    sites[::11, 0] = -1.0
+    c0, c1 = cases.random_field(w, h, n, seed)
+    gout = np.random.default_rng(seed).normal(size=(h, w, 3)).astype(np.float32)
+    got = ops.render_sad_backward(t32(c0), t32(c1), tf(sites), tf(gout), 1.0 / max(w, h) ** 2, w, h)
+    want, absw = orc.render_backward(c0, c1, sites, gout, w, h)
+    got = got.cpu().numpy().astype(np.float64)
+    assert np.all(np.abs(got - want) <= 1e-3 * absw + 1e-6)
+
+
+def test_autograd_function_and_fp64_finite_differences(cuda, orc):
+    """SADRenderFunction's backward against central differences (h = 1e-6) of the FP64
+    forward on all per-site parameters (64x64, 256 sites, candidates fixed)."""
+    from sad_gb300 import SADRenderFunction
+    import test_oracle_cpu as t
+    w = h = 64
+    img, sites = cases.scene(w, h, 256, seed=3)
+    sites[:, 2] = 3.0
+    c0, c1 = cases.knn_field(sites, w, h)
+    inv_s2 = 1.0 / (w * w)
+    gout = np.random.default_rng(1).normal(size=(h, w, 3))
+    s_t = tf(sites).requires_grad_(True)
+    out = SADRenderFunction.apply(s_t, t32(c0), t32(c1), inv_s2, w, h)
+    out.backward(tf(gout))
+    g = s_t.grad.cpu().numpy().astype(np.float64)
+    s64 = sites.astype(np.float64)
+    loss = lambda s: float(np.sum(orc.render_d(c0, c1, s, w, h, inv_s2) * gout))
+    # FP32 adjoint vs FP64 differences: the relative gradient tolerance is 1e-3
+    worst = t.fd_gradcheck(loss, s64, g, np.random.default_rng(2).choice(256, 16, replace=False),
+                           rtol=1e-3)
+    assert worst < 2e-3, worst
+    _, absw = orc.render_backward(c0, c1, sites, gout.astype(np.float32), w, h)
+    g64 = orc.render_backward_d(c0, c1, s64, gout, w, h, inv_s2)
+    assert np.all(np.abs(g - g64) <= 1e-3 * absw + 1e-6)
+
+
+# ---------------------------------------------------------------------------
+# candidates
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("w,h,n,per_pixel", [(64, 32, 1000, False), (37, 21, 37 * 21, True),
+                                             (16, 16, 0, False)])
+def test_init_candidates_bit_exact(ops, orc, w, h, n, per_pixel):
+    a, b = ops.init_candidates(w, h, n, 12345)
+    want = orc.init_candidates(n, 12345, per_pixel, w, h)
+    np.testing.assert_array_equal(u32(a), want[0])
+    np.testing.assert_array_equal(u32(b), want[1])
+
+
+def test_pack_bit_exact(ops, orc):
+    img, sites = cases.scene(64, 64, 5000, 7)
+    sites[::7, 0] = -1
+    sites[1, :] = [65519.99, 1e-9, 1e5, -3, 1, 1, 1, 0.3, -0.2, 7.0]
+    packed = torch.zeros((5000, 8), dtype=torch.float16, device="cuda")
+    ops.pack_candidate_sites(tf(sites), packed, 0)
+    np.testing.assert_array_equal(packed.cpu().numpy().view(np.uint16), orc.pack_sites(sites))
+
+
+def test_jfa_seed_lowest_id_wins(ops, orc):
+    w, h, n = 40, 30, 900  # more sites than texels: collisions
+    img, sites = cases.scene(w, h, n, 8)
+    sites[::5, 0] = -1
+    c0 = np.random.default_rng(0).integers(0, n, (w * h, 4)).astype(np.uint32)
+    got = ops.jfa_seed(t32(c0), tf(sites), 0, 1, w, h)
+    np.testing.assert_array_equal(u32(got), orc.jfa_seed(c0, sites, w, h))
+
+
+@pytest.mark.parametrize("ds", [1, 2])
+def test_jfa_flood_matches_oracle(ops, orc, ds):
+    """Each flood pass compared on its own (both sides start from the oracle's field)."""
+    w, h, n = 80, 56, 600
+    tw, th = w * ds, h * ds
+    img, sites = cases.scene(tw, th, n, 9)
+    sites[::9, 0] = -1
+    inv = 1.0 / max(tw, th) ** 2
+    field = orc.jfa_seed(np.full((w * h, 4), U32, np.uint32), sites, w, h, ds)
+    dist = lambda ids, xs, ys: raw_dist_np(sites, ids, np.minimum(xs * ds, tw - 1),
+                                           np.minimum(ys * ds, th - 1), inv)
+    for step in (64, 32, 16, 8, 4, 2, 1):
+        out = torch.empty((w * h, 4), dtype=torch.int32, device="cuda")
+        got = u32(ops.jfa_flood(t32(field), out, tf(sites), inv, 0, step, ds, w, h))
+        want = orc.jfa_flood(field, sites, step, w, h, ds)
+        assert_lists_match(got, want, dist, w, h)
+        field = want
+
+
+@pytest.mark.parametrize("w,h,n,hil,seed", [(96, 64, 800, True, 10), (257, 129, 6000, True, 11),
+                                            (50, 50, 300, False, 12)])
+def test_vpt_pass_matches_oracle(ops, orc, w, h, n, hil, seed):
+    img, sites = cases.scene(w, h, n, seed)
+    sites[::10, 0] = -1
+    c0, c1 = cases.random_field(w, h, n, seed)
+    packed_np = orc.pack_sites(sites)
+    inv = 1.0 / max(w, h) ** 2
+    horder = hpos = None
+    hp = hw = 0
+    if hil:
+        bits = orc.hilbert_bits_for_size(w, h)
+        padded = (n + 1023) // 1024 * 1024
+        pairs = orc.hilbert_pairs(sites, padded, w, h, bits)
+        pairs = orc.radix_sort_pairs(pairs, 0xFFFFFFFF if bits >= 16 else 1 << (2 * bits))
+        horder, hpos = orc.hilbert_order(pairs, n)
+        hp, hw = 1, 32
+    packed = torch.from_numpy(packed_np.view(np.float16)).cuda()
+    ho = t32(horder) if hil else torch.zeros(1, dtype=torch.int32, device="cuda")
+    hps = t32(hpos) if hil else torch.zeros(1, dtype=torch.int32, device="cuda")
+    for idx in (0, 3, 9, 70000):
+        step = orc.pack_jump_step(idx, w, h)
+        o0, o1 = torch.empty((w * h, 4), dtype=torch.int32, device="cuda"), torch.empty((w * h, 4), dtype=torch.int32, device="cuda")
+        ops.update_candidates_compact(t32(c0), t32(c1), o0, o1, packed, ho, hps, inv, n, step, idx >> 16,
+                                      64.0, 0, 4, hp, hw, 1, w, h, w, h)
+        w0, w1 = orc.vpt_pass(c0, c1, packed_np, n, step, idx >> 16, w, h, 64.0, 0, 4, horder, hpos, hp, hw)
+        got = np.concatenate([u32(o0), u32(o1)], axis=1)
+        want = np.concatenate([w0, w1], axis=1)
+        assert_lists_match(got, want, lambda ids, xs, ys: packed_dist_np(sites, ids, xs, ys, inv), w, h)
+
+
+def test_vpt_pass_op(ops, orc):
+    w, h, n = 48, 40, 500
+    img, sites = cases.scene(w, h, n, 13)
+    c0, c1 = cases.random_field(w, h, n, 13)
+    inv = 1.0 / w ** 2
+    o0, o1 = ops.vpt_pass(t32(c0), t32(c1), tf(sites), inv, w, h, 16, 0, 1.0, 3, 0)
+    w0, w1 = orc.vpt_pass(c0, c1, orc.pack_sites(sites), n, 16 << 16, 0, w, h, 1.0, 0, 3)
+    got = np.concatenate([u32(o0), u32(o1)], axis=1)
+    want = np.concatenate([w0, w1], axis=1)
+    assert_lists_match(got, want, lambda ids, xs, ys: packed_dist_np(sites, ids, xs, ys, inv), w, h)
+
+
+# ---------------------------------------------------------------------------
+# training kernels
+# ---------------------------------------------------------------------------
+def _grad_buffers(n):
+    return [torch.zeros(n, dtype=torch.float32, device="cuda") for _ in range(11)]
+
+
+@pytest.mark.parametrize("w,h,n,removal,masked,ssim", [
+    (64, 64, 400, False, False, 0.0), (97, 61, 900, True, False, 0.0),
+    (128, 128, 2000, True, True, 0.0), (72, 40, 300, False, False, 0.2)])
+def test_fused_gradients_match_oracle(ops, orc, w, h, n, removal, masked, ssim):
+    img, sites = cases.scene(w, h, n, 20 + n)
+    sites[::9, 0] = -1
+    c0, c1 = cases.random_field(w, h, n, 21)
+    mask = np.ones((h, w), np.float32)
+    if masked:
+        mask[h // 3: h // 2, :] = 0.0
+    rendered = orc.render(c0, c1, sites, w, h)
+    bufs = _grad_buffers(n)
+    ops.compute_gradients_tiled(t32(c0), t32(c1), tf(img), tf(rendered), tf(mask), tf(sites), *bufs,
+                                1.0 / max(w, h) ** 2, 0, int(removal), ssim, w, h)
+    g, a, rem = orc.compute_gradients(c0, c1, img, sites, w, h, mask=mask if masked else None,
+                                      rendered=rendered, ssim_weight=ssim, removal=removal)
+    got = np.stack([b.cpu().numpy() for b in bufs[:10]]).astype(np.float64)
+    assert np.all(np.abs(got - g) <= 1e-3 * a + 1e-6)
+    if removal:
+        r = bufs[10].cpu().numpy().astype(np.float64)
+        assert np.all(np.abs(r - rem) <= 1e-3 * np.maximum(np.abs(rem), 1.0) + 1e-4)
+
+
+def test_tau_diffuse_matches_oracle(ops, orc):
+    w, h, n = 64, 48, 700
+    img, sites = cases.scene(w, h, n, 30)
+    sites[::6, 0] = -1
+    c0, c1 = cases.random_field(w, h, n, 30)
+    rng = np.random.default_rng(0)
+    raw = rng.normal(size=n).astype(np.float32)
+    gin = rng.normal(size=n).astype(np.float32)
+    out = torch.empty(n, dtype=torch.float32, device="cuda")
+    ops.tau_diffuse(t32(c0), t32(c1), tf(sites), tf(raw), tf(gin), out, 0, 0.037, 1, w, h)
+    want = orc.tau_diffuse(c0, c1, sites, raw, gin, 0.037, w, h)
+    np.testing.assert_allclose(out.cpu().numpy(), want, rtol=1e-6, atol=1e-7)
+
+
+def test_adam_matches_oracle(ops, orc):
+    n, w, h = 1000, 200, 150
+    img, sites = cases.scene(w, h, n, 31)
+    sites[::8, 0] = -1
+    rng = np.random.default_rng(1)
+    grads = rng.normal(size=(10, n)).astype(np.float32) * 50
+    adam = (rng.random((n, 20)) * 1e-3).astype(np.float32)
+    lr = [0.025, 0.01, 0.01, 0.01, 0.0025, 0.025]
+    s_t, a_t = tf(sites), tf(adam)
+    ops.adam_update(s_t, a_t, *[tf(g) for g in grads], *lr, 0.9, 0.999, 1e-8, 7, w, h)
+    ws, wa = orc.adam_update(sites, adam, grads, lr, 0.9, 0.999, 1e-8, 7, w, h)
+    np.testing.assert_allclose(s_t.cpu().numpy(), ws, rtol=2e-6, atol=2e-6)
+    np.testing.assert_allclose(a_t.cpu().numpy(), wa, rtol=2e-6, atol=1e-9)
+
+
+@pytest.mark.parametrize("case", cases.sort_cases(include_large=True), ids=lambda c: c[0])
+def test_radix_sort_bit_exact(ops, case):
+    name, pairs, max_key, count = case
+    p = t32(pairs)
+    ops.radix_sort_pairs(p, max_key)
+    np.testing.assert_array_equal(u32(p), cases.expected_sort(pairs, max_key))
+
+
+def test_prune_pipeline_bit_exact(ops, orc):
+    n, pc = 5000, 5120
+    img, sites = cases.scene(64, 64, n, 40)
+    sites[::10, 0] = -1
+    rem = np.random.default_rng(5).normal(size=n).astype(np.float32)
+    rem[::17] = np.inf
+    pairs = torch.zeros((pc, 2), dtype=torch.int32, device="cuda")
+    ops.compute_prune_score_pairs(tf(sites), tf(rem), pairs, 0, 1.0 / 4096, pc)
+    want_pairs = orc.prune_pairs(sites, rem, pc, 1.0 / 4096)
+    np.testing.assert_array_equal(u32(pairs), want_pairs)
+    ops.radix_sort_pairs(pairs, U32)
+    srt = orc.radix_sort_pairs(want_pairs, U32)
+    np.testing.assert_array_equal(u32(pairs), srt)
+    k = 300
+    idx = torch.zeros(65536, dtype=torch.int32, device="cuda")
+    ops.write_split_indices(pairs, idx, k)
+    s_t = tf(sites)
+    ops.prune_sites(s_t, idx, k)
+    np.testing.assert_array_equal(s_t.cpu().numpy(), orc.prune_sites(sites, srt[:k, 1]))
+
+
+def test_densify_pairs_and_split(ops, orc):
+    w, h, n = 96, 80, 600
+    img, sites = cases.scene(w, h, n, 41)
+    c0, c1 = cases.knn_field(sites, w, h)
+    st = [torch.zeros(n + 100, dtype=torch.float32, device="cuda") for _ in range(8)]
+    ops.compute_site_stats_tiled(t32(c0), t32(c1), tf(img), tf(np.ones((h, w), np.float32)), tf(sites), *st,
+                                 1.0 / w ** 2, n, w, h)
+    want = orc.site_stats(c0, c1, img, sites, w, h)
+    got = np.stack([s.cpu().numpy()[:n] for s in st]).astype(np.float64)
+    np.testing.assert_allclose(got, want, rtol=2e-4, atol=1e-4)
+    pairs = torch.zeros((n, 2), dtype=torch.int32, device="cuda")
+    ops.compute_densify_score_pairs(tf(sites), st[0], st[1], pairs, n, 1.0, 0.7, n)
+    wp = orc.densify_pairs(sites, got[0].astype(np.float32), got[1].astype(np.float32), n, 1.0, 0.7)
+    gp = u32(pairs)
+    np.testing.assert_array_equal(gp[:, 1], wp[:, 1])
+    # keys come from powf: CPU and GPU may round the score one ulp apart
+    assert np.all(np.abs(gp[:, 0].astype(np.int64) - wp[:, 0].astype(np.int64)) <= 2)
+    k = 50
+    idx = np.arange(0, 2 * k, 2, dtype=np.uint32)
+    big = np.zeros((n + 100, 10), np.float32)
+    big[:n] = sites
+    adam = np.ones((n + 100, 20), np.float32)
+    s_t, a_t = tf(big), tf(adam)
+    stats7 = [got[0], got[2], got[3], got[4], got[5], got[6], got[7]]
+    ops.split_sites(s_t, a_t, t32(idx), *[tf(x) for x in stats7], n, k, tf(img))
+    ws, wa = orc.split_sites(big, adam, idx, stats7, n, img, w, h)
+    np.testing.assert_allclose(s_t.cpu().numpy(), ws, rtol=1e-4, atol=2e-4)
+    np.testing.assert_array_equal(a_t.cpu().numpy(), wa)
+
+
+def test_hilbert_order_bit_exact(ops, orc):
+    w, h, n = 300, 200, 7000
+    img, sites = cases.scene(w, h, n, 50)
+    bits = orc.hilbert_bits_for_size(w, h)
+    padded = (n + 1023) // 1024 * 1024
+    pairs = torch.zeros((padded, 2), dtype=torch.int32, device="cuda")
+    ops.build_hilbert_pairs(tf(sites), pairs, n, padded, w, h, bits)
+    wp = orc.hilbert_pairs(sites, padded, w, h, bits)
+    np.testing.assert_array_equal(u32(pairs), wp)
+    mk = 0xFFFFFFFF if bits >= 16 else 1 << (2 * bits)
+    ops.radix_sort_pairs(pairs, mk)
+    order = torch.zeros(n, dtype=torch.int32, device="cuda")
+    pos = torch.zeros(n, dtype=torch.int32, device="cuda")
+    ops.write_hilbert_order(pairs, order, pos, n)
+    wo, wpos = orc.hilbert_order(orc.radix_sort_pairs(wp, mk), n)
+    np.testing.assert_array_equal(u32(order), wo)
+    np.testing.assert_array_equal(u32(pos), wpos)
+
+
+@pytest.mark.parametrize("w,h,n,masked", [(128, 96, 3000, False), (256, 256, 20000, True)])
+def test_init_gradient_weighted_matches_oracle(ops, orc, w, h, n, masked):
+    img, _ = cases.scene(w, h, 1, 60)
+    mask = np.ones((h, w), np.float32)
+    if masked:
+        mask[:, : w // 2] = 0.0
+    s = torch.zeros((n, 10), dtype=torch.float32, device="cuda")
+    ops.init_gradient_weighted(s, tf(img), tf(mask), n, 5.0, 4.0, 1.0)
+    want = orc.init_gradient_weighted(img, n, 0.01, 256, 5.0, 4.0, mask)
+    got = s.cpu().numpy()
+    cols = [0, 1, 3, 4, 5, 6, 7, 8, 9]
+    np.testing.assert_array_equal(got[:, cols], want[:, cols])
+    np.testing.assert_allclose(got[:, 2], want[:, 2], rtol=1e-6)
+
+
+def test_metrics_match_oracle(cuda, orc):
+    from sad_gb300 import _lib
+    import ctypes as C
+    w, h = 200, 123
+    rng = np.random.default_rng(3)
+    a, b = rng.random((h, w, 3), dtype=np.float32), rng.random((h, w, 3), dtype=np.float32)
+    mask = (rng.random((h, w)) > 0.2).astype(np.float32)
+    acc = torch.zeros(2, dtype=torch.float32, device="cuda")
+    p = lambda t: C.c_void_p(t.data_ptr())
+    at, bt, mt = tf(a), tf(b), tf(mask)
+    _lib.call("sad_compute_mse", p(at), p(bt), p(mt), p(acc), w, h, None)
+    _lib.call("sad_compute_ssim", p(at), p(bt), p(mt), C.c_void_p(acc.data_ptr() + 4), w, h, None)
+    torch.cuda.synchronize()
+    mse = float(np.sum(((a - b) ** 2).sum(-1) * (mask > 0)))
+    assert abs(acc[0].item() - mse) <= 1e-4 * mse
+    assert abs(acc[1].item() - orc.ssim_sum(a, b, mask)) <= 1e-3 * abs(orc.ssim_sum(a, b, mask)) + 1e-3
+    img, sites = cases.scene(64, 64, 999, 1)
+    sites[::3, 0] = -1
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = tf(sites)
+    _lib.call("sad_count_active_sites", p(st), p(cnt), 999, None)
+    assert cnt.item() == orc.count_active(sites)
+
+
+def test_ops_use_current_stream(ops, orc):
+    w, h, n = 64, 64, 500
+    img, sites = cases.scene(w, h, n, 70)
+    c0, c1 = cases.random_field(w, h, n, 70)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        out = ops.render_sad(t32(c0), t32(c1), tf(sites), 1.0 / w ** 2, w, h)
+    s.synchronize()
+    assert np.max(np.abs(out.cpu().numpy() - orc.render(c0, c1, sites, w, h))) <= 1e-4
+
+
+def test_torch_ops_dispatch(cuda, orc):
+    import sad_gb300  # noqa: F401  (registers torch.ops.sad)
+    from sad_gb300 import torch_ops
+    torch_ops.register()
+    w, h, n = 40, 30, 100
+    img, sites = cases.scene(w, h, n, 71)
+    c0, c1 = torch.ops.sad.init_candidates(w, h, n, 5)
+    out = torch.ops.sad.render_sad(c0, c1, tf(sites), 1.0 / w ** 2, w, h)
+    want = orc.render(u32(c0), u32(c1), sites, w, h)
+    assert np.max(np.abs(out.cpu().numpy() - want)) <= 1e-4
