@@ -296,6 +296,23 @@ def run_reference(args):
             "note": "the reference's path is CUDA-only; this is the CPU restatement of its kernels"}
 
 
+def run_profile(args):
+    """Eager (graph-free) fit of the workload for `--profile-iters` iterations, so every
+    kernel is a separate launch for ncu; nothing is timed."""
+    import torch
+    from sad_gb300.synthetic import synthetic_image
+    from sad_gb300.trainer import Trainer
+    img = synthetic_image(WIDTH, HEIGHT, seed=0)
+    tr = Trainer(WIDTH, HEIGHT, log_freq=0, use_graphs=0)
+    tr.set_target(torch.from_numpy(img).cuda())
+    tr.init()
+    tr.run(args.profile_iters)
+    torch.cuda.synchronize()
+    print(json.dumps({"mode": "profile", "iterations": args.profile_iters, "psnr_db": tr.psnr()}))
+    tr.close()
+    return None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -304,7 +321,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
+    ap.add_argument("--profile-iters", type=int, default=200)
     args = ap.parse_args()
+    if args.mode == "profile":
+        run_profile(args)
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out is not None:

@@ -1,0 +1,16 @@
+#!/usr/bin/env bash
+# Copy the reference's CUDA backend sources (kernels, host driver, vendored IO headers,
+# training_config.json) from the read-only reference checkout into baseline/_ref/, the
+# git-ignored location for the reference that travels with the repository snapshot to the
+# GPU machine.  Nothing here is committed; oracle/ref/build.sh compiles from that copy.
+#   usage: oracle/ref/stage.sh [/path/to/reference]
+set -euo pipefail
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")/../.." && pwd)
+DST="$HERE/baseline/_ref/sad"
+rm -rf "$DST"
+mkdir -p "$DST"
+cp -r "$REF/backends/cuda/src" "$DST/src"
+cp -r "$REF/backends/cuda/third_party" "$DST/third_party"
+cp "$REF/training_config.json" "$DST/"
+echo "staged $(ls "$DST/src" | wc -l) files into $DST"

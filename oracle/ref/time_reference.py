@@ -1,0 +1,99 @@
+"""Time the reference's own CUDA CLI on the benchmark workload and this library's trainer on
+the identical 8-bit image (equal-PSNR speed comparison).  Prints one JSON line.
+
+    oracle/ref/stage.sh /path/to/reference && oracle/ref/build.sh
+    python oracle/ref/time_reference.py [--repeats 2] [--size 1024]
+
+The reference binary (oracle/_ref/sad_cuda, built from the staged copy of its sources)
+reads training_config.json from its working directory (baseline/_ref/sad holds the staged
+one) and prints "Iter N | PSNR: x dB | Active: a/n | r it/s | t s" lines; its it/s is
+iterations / seconds since the end of its initialisation.  Ours is timed the same way
+(init excluded), with CUDA events around the training loop.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [ROOT]
+
+
+def run_reference(png: str, repeats: int, log_freq: int):
+    exe = os.path.join(ROOT, "oracle", "_ref", "sad_cuda")
+    cwd = os.path.join(ROOT, "baseline", "_ref", "sad")
+    best = None
+    for _ in range(repeats):
+        out_dir = tempfile.mkdtemp()
+        t0 = time.perf_counter()
+        r = subprocess.run([exe, png, "--log-freq", str(log_freq), "--out-dir", out_dir], cwd=cwd,
+                           capture_output=True, text=True, timeout=1800)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0:
+            raise RuntimeError(f"reference CLI failed: {r.stdout[-2000:]} {r.stderr[-2000:]}")
+        its = [float(m) for m in re.findall(r"\|\s*([0-9.]+) it/s", r.stdout)]
+        psnr = re.findall(r"Final PSNR: ([0-9.]+)", r.stdout)
+        ttime = re.findall(r"Training time: ([0-9.]+) s", r.stdout)
+        act = re.findall(r"Active: (\d+)/(\d+)", r.stdout)
+        res = {"it_per_s": its[-1] if its else None, "psnr_db": float(psnr[-1]) if psnr else None,
+               "training_time_s": float(ttime[-1]) if ttime else None, "wall_s": round(wall, 3),
+               "active_final": int(act[-1][0]) if act else None, "log": r.stdout.splitlines()[-12:]}
+        if best is None or (res["it_per_s"] or 0) > (best["it_per_s"] or 0):
+            best = res
+    return best
+
+
+def run_ours(img, repeats: int):
+    import torch
+    from sad_gb300.trainer import Trainer
+    h, w = img.shape[:2]
+    tr = Trainer(w, h, log_freq=0)
+    tr.set_target(torch.from_numpy(img).cuda())
+    from sad_gb300 import _lib
+    stream = torch.cuda.ExternalStream(_lib.load().sad_trainer_stream(tr._h))
+    best = None
+    for _ in range(repeats + 1):  # first fit warms up
+        tr.init()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        tr.run()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        res = {"it_per_s": tr.cfg.iterations / (ms / 1e3), "psnr_db": tr.psnr(),
+               "training_time_s": ms / 1e3, "active_final": int(tr.sites().shape[0])}
+        if best is None or res["it_per_s"] > best["it_per_s"]:
+            best = res
+    tr.close()
+    return best
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--repeats", type=int, default=2)
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--log-freq", type=int, default=1000)
+    args = ap.parse_args()
+    from sad_gb300 import imageio
+    from sad_gb300.synthetic import quantize_u8, synthetic_image
+    img = quantize_u8(synthetic_image(args.size, args.size, seed=0))
+    png = os.path.join(tempfile.mkdtemp(), f"synthetic_{args.size}.png")
+    imageio.save_image(png, img)
+    ref = run_reference(png, args.repeats, args.log_freq)
+    ours = run_ours(img, args.repeats)
+    out = {"workload": f"{args.size}x{args.size} synthetic (8-bit), training_config.json defaults",
+           "reference_cuda_cli": ref, "ours": ours,
+           "speedup_it_per_s": round(ours["it_per_s"] / ref["it_per_s"], 2) if ref.get("it_per_s") else None}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

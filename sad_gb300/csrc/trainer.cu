@@ -478,9 +478,10 @@ static sad_status_t set_mask_common(sad_trainer* t, bool have_mask) {
     SAD_TRY(check_cuda(cudaMemcpyAsync(host.data(), t->mask, host.size() * 4, cudaMemcpyDeviceToHost, t->st),
                        "trainer mask readback"));
     SAD_TRY(check_cuda(cudaStreamSynchronize(t->st), "trainer mask sync"));
-    double sum = 0.0;
-    for (float v : host) sum += v;
-    t->mask_sum = static_cast<float>(sum);
+    // the reference counts the pixels with mask > 0 (backends/cuda/src/sad_cuda.cu:208-213)
+    size_t live = 0;
+    for (float v : host) live += v > 0.0f;
+    t->mask_sum = static_cast<float>(live);
     return SAD_OK;
 }
 
@@ -612,6 +613,7 @@ extern "C" sad_status_t sad_trainer_run(sad_trainer_t* t, int end) {
             if (p.upd) t->cur = refresh_target(t, t->cur);
         }
         SAD_TRY(check_launch("sad_trainer_run"));
+        if (p.prune) t->active = std::max(0, t->active - static_cast<int>(p.prune_k));
         t->iter = it + 1;
         if (c.log_freq > 0 && (it % c.log_freq == 0 || it == c.iterations - 1))
             SAD_TRY(log_iteration(t, it));

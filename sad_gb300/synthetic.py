@@ -86,4 +86,5 @@ def synthetic_sites(image: np.ndarray, n: int, seed: int = 0, log_tau: float = 5
 
 def quantize_u8(image: np.ndarray) -> np.ndarray:
     """The 8-bit image a PNG-reading caller would see, back in [0,1] float32."""
-    return (np.round(np.clip(image, 0, 1) * 255.0) / 255.0).astype(np.float32)
+    u8 = np.round(np.clip(image, 0, 1) * 255.0).astype(np.float32)
+    return u8 / np.float32(255.0)

