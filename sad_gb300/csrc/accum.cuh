@@ -1,85 +1,250 @@
-// accum.cuh -- per-tile accumulation of per-site values (gradients, removal deltas).
+// accum.cuh -- per-tile accumulation of per-site values (gradients, removal deltas,
+// statistics).
 //
 // The reference accumulates every (pixel, candidate) contribution with one shared-memory
-// atomic per value into a 256-slot hash per 16x16 tile, falling back to global atomics
-// (backends/cuda/src/gradients.cu:422-485).  Neighbouring pixels share most of their
-// candidates, so those shared atomics collide on the same address.
+// float atomic per value into a 256-slot hash per 16x16 tile, falling back to global
+// atomics (backends/cuda/src/gradients.cu:422-485).  Neighbouring pixels share most of
+// their candidates, often in the same slot order, so a warp's 32 lanes hit the same
+// address and the atomics serialise.
 //
-// Here each warp first merges the contributions of its lanes that carry the same site:
-// __match_any_sync groups the lanes by key and a segmented tree reduction over
-// shuffles (log2 of the largest group rounds) leaves each group's sum in its lowest
-// lane.  Only those leaders touch the shared hash, so the shared atomics of a warp go
-// to distinct slots.  Keys that do not fit the table within kMaxProbe probes go straight
-// to global memory through the caller's fallback.
+// Here a tile table is filled in two steps:
+//   1. registration: for each candidate slot, __match_any_sync groups the warp's lanes by
+//      site; the group's lowest lane inserts the key (CAS probe) and broadcasts the table
+//      slot, so each key costs one CAS per warp;
+//   2. accumulation: every lane adds its values to the registered slot directly, visiting
+//      its 8 candidates in a lane-rotated order so lanes with identical lists hit
+//      different slots at the same instruction.
+// Values are accumulated either as float (API calls, which add into caller buffers like
+// the reference) or as fixed point (the trainer): integer addition is associative, so
+// per-site sums -- and with them whole fits -- are bitwise reproducible.  Keys that do not
+// fit within kMaxProbe probes go to global memory through the caller's fallback, which
+// adds the same integers.
 #pragma once
 
 #include "common.cuh"
 
 namespace sad {
 
-template <int NV, int SLOTS>
-struct TileTable {
+// Fixed point with 28 fractional bits (resolution 3.7e-9) in 64-bit global records
+// (range +-3.4e10 per site).
+constexpr int kFixFracBits = 28;
+constexpr float kFixScale = 268435456.0f;                 // 2^28
+constexpr float kFixInvScale = 3.7252902984619141e-09f;  // 2^-28
+// Per tile, a fixed-point sum is kept as two 32-bit words (hi * 2^20 + lo): shared
+// memory has native 32-bit integer atomics but no native 64-bit add.  Exact while a tile's
+// sum of one value stays below 2^23 in magnitude (and each term below 2^23).
+constexpr int kSplitLoBits = 20;
+
+__device__ __forceinline__ long long to_fix(float v) { return __float2ll_rn(v * kFixScale); }
+__host__ __device__ __forceinline__ float from_fix(long long v) {
+#ifdef __CUDA_ARCH__
+    return __ll2float_rn(v) * kFixInvScale;
+#else
+    return static_cast<float>(v) * kFixInvScale;
+#endif
+}
+
+__device__ __forceinline__ void fix_add_global(long long* p, long long v) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v));
+}
+
+// Split of to_fix(v) = h * 2^20 + l with |l| <= 2^19, in FP32 and INT32 arithmetic (a float
+// -> 64-bit integer conversion runs on the FP64 pipe).  With y = v * 2^8 (exact), adding
+// 1.5 * 2^23 rounds y to the nearest integer yr in the low mantissa bits; r = y - yr is exact
+// and |r| <= 1/2, and rounding r * 2^20 the same way gives l.  h * 2^20 + l is then
+// round-half-even(v * 2^28), the integer to_fix() gives for the global path.  h is 0 for
+// |v| < 2^-9.  |v| < 2^14 takes this path; larger terms (to 2^23) split exactly via F2I.
+__device__ __forceinline__ void split_fix(float v, int& h, int& l) {
+    const float kMagic = 12582912.0f;  // 1.5 * 2^23
+    const int kMagicBits = 0x4B400000;
+    if (fabsf(v) < 16384.0f) {
+        float y = v * 256.0f;
+        float ym = y + kMagic;
+        float r = y - (ym - kMagic);
+        h = __float_as_int(ym) - kMagicBits;
+        l = __float_as_int(fmaf(r, 1048576.0f, kMagic)) - kMagicBits;
+    } else {
+        float y = v * 256.0f;  // an integer for |v| >= 2^15; otherwise split its fraction
+        float yf = truncf(y);
+        h = __float2int_rz(yf);
+        l = __float2int_rn((y - yf) * 1048576.0f);
+    }
+}
+
+// Accumulation modes of a tile table.
+struct AccFloat {};  // float shared atomics (order-dependent rounding, like the reference)
+struct AccSplit {};  // exact fixed point (hi, lo) words: bitwise reproducible sums
+
+// Key -> dense index map of one tile.  Keys live in an open-addressing hash; each newly
+// claimed key gets the next dense index, so the value arrays are packed: keys registered
+// together sit in consecutive (bank-distinct) words, and the flush visits only used
+// entries.
+template <int SLOTS>
+struct KeyTable {
     static_assert((SLOTS & (SLOTS - 1)) == 0, "SLOTS must be a power of two");
     static constexpr int kMaxProbe = 16;
+    static constexpr int kSpinLimit = 1 << 20;
     uint32_t keys[SLOTS];
-    float vals[NV][SLOTS];
+    int dense[SLOTS];      // dense index of hash slot s, -1 until its claimer publishes it
+    uint32_t dkey[SLOTS];  // key of dense index d
+    int count;
 
-    __device__ __forceinline__ void init(int tid, int nthreads) {
+    __device__ __forceinline__ void init_keys(int tid, int nthreads) {
         for (int i = tid; i < SLOTS; i += nthreads) {
             keys[i] = kEmpty;
-#pragma unroll
-            for (int k = 0; k < NV; ++k) vals[k][i] = 0.0f;
+            dense[i] = -1;
         }
+        if (tid == 0) count = 0;
     }
 
-    __device__ __forceinline__ static uint32_t home(uint32_t key) {
-        return (key * 2654435761u) & (SLOTS - 1);
-    }
-
-    // Add v to the slot of `key`; returns false when the table is full along the probe run.
-    __device__ __forceinline__ bool add(uint32_t key, const float (&v)[NV]) {
-        uint32_t h = home(key);
+    // Dense index of `key` (inserting it), or -1 when the probe run is full.  A thread that
+    // finds the key claimed by another warp waits (bounded) for its index; past the bound
+    // it reports -1 and the caller takes the global path.
+    __device__ __forceinline__ int insert(uint32_t key) {
+        uint32_t h = (key * 2654435761u) & (SLOTS - 1);
 #pragma unroll 1
         for (int p = 0; p < kMaxProbe; ++p) {
             uint32_t s = (h + p) & (SLOTS - 1);
             uint32_t old = atomicCAS(&keys[s], kEmpty, key);
-            if (old == kEmpty || old == key) {
-#pragma unroll
-                for (int k = 0; k < NV; ++k) atomicAdd(&vals[k][s], v[k]);
-                return true;
+            if (old == kEmpty) {
+                int d = atomicAdd(&count, 1);
+                dkey[d] = key;
+                __threadfence_block();
+                atomicExch(&dense[s], d);
+                return d;
+            }
+            if (old == key) {
+                volatile int* ds = &dense[s];
+#pragma unroll 1
+                for (int it = 0; it < kSpinLimit; ++it) {
+                    int d = *ds;
+                    if (d >= 0) return d;
+                }
+                return -1;
             }
         }
-        return false;
+        return -1;
+    }
+
+    __device__ __forceinline__ int size() const { return count; }
+    __device__ __forceinline__ uint32_t key_at(int d) const { return dkey[d]; }
+};
+
+template <int NV, int SLOTS, class Mode>
+struct TileTable;
+
+template <int NV, int SLOTS>
+struct TileTable<NV, SLOTS, AccFloat> : KeyTable<SLOTS> {
+    float vals[NV][SLOTS];
+
+    __device__ __forceinline__ void init(int tid, int nthreads) {
+        this->init_keys(tid, nthreads);
+        for (int i = tid; i < SLOTS; i += nthreads) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) vals[k][i] = 0.0f;
+        }
+    }
+    __device__ __forceinline__ void add(int d, const float (&v)[NV]) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) atomicAdd(&vals[k][d], v[k]);
+    }
+    __device__ __forceinline__ float value(int k, int d) const { return vals[k][d]; }
+    __device__ __forceinline__ long long fixed(int k, int d) const { return to_fix(vals[k][d]); }
+};
+
+// Fixed-point words: x = to_fix(v) = hi * 2^20 + lo with |lo| <= 2^19, so the lo sum of
+// up to 2^11 terms fits an int32 and hi (zero for |v| < 2^-9, then skipped) wraps modulo
+// 2^32, which the recombination absorbs while the tile's total stays below 2^23.
+template <int NV, int SLOTS>
+struct TileTable<NV, SLOTS, AccSplit> : KeyTable<SLOTS> {
+    int hi[NV][SLOTS];
+    int lo[NV][SLOTS];
+
+    __device__ __forceinline__ void init(int tid, int nthreads) {
+        this->init_keys(tid, nthreads);
+        for (int i = tid; i < SLOTS; i += nthreads) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                hi[k][i] = 0;
+                lo[k][i] = 0;
+            }
+        }
+    }
+    __device__ __forceinline__ void add(int d, const float (&v)[NV]) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            int h, l;
+            split_fix(v[k], h, l);
+            atomicAdd(&lo[k][d], l);
+            if (h != 0) atomicAdd(&hi[k][d], h);
+        }
+    }
+    __device__ __forceinline__ long long fixed(int k, int d) const {
+        return static_cast<long long>(hi[k][d]) * (1ll << kSplitLoBits) + static_cast<long long>(lo[k][d]);
     }
 };
 
-// Segmented sum over the lanes of a warp that hold the same key.  Must be called by all
-// 32 lanes.  On return the lowest lane of every key group holds the group's sums and
-// `leader` is true there.
-template <int NV>
-__device__ __forceinline__ bool warp_merge_by_key(uint32_t key, float (&v)[NV]) {
-    const uint32_t full = 0xffffffffu;
-    uint32_t lane = lane_id();
-    uint32_t lt = lanemask_lt();
-    uint32_t peers = __match_any_sync(full, key);
-    bool leader = (peers & lt) == 0u;
-    uint32_t rank = __popc(peers & lt);
-    uint32_t above = peers & ~(lt | (1u << lane));
-    // Round r: every lane adds the value of its next remaining higher peer; the lanes
-    // of odd rank are then absorbed and drop out of all peer sets.
-    while (__any_sync(full, above != 0u)) {
-        int next = __ffs(above) - 1;
-        int src = next < 0 ? static_cast<int>(lane) : next;
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            float t = __shfl_sync(full, v[k], src);
-            if (next >= 0) v[k] += t;
-        }
-        uint32_t absorbed = __ballot_sync(full, (rank & 1u) != 0u);
-        above &= ~absorbed;
-        rank >>= 1;
-    }
-    return leader;
+// The table lives in dynamic shared memory (the 64-bit variants exceed the 48 KB static
+// limit); launches pass sizeof(Table) and opt in through allow_dynamic_smem().
+template <class Table>
+__device__ __forceinline__ Table& shared_table() {
+    extern __shared__ __align__(16) unsigned char sad_dyn_smem[];
+    return *reinterpret_cast<Table*>(sad_dyn_smem);
 }
+
+// Step 1 for one candidate slot: all 32 lanes call it (key = kEmpty for none); returns the
+// dense table index of the lane's key (-1: no key or table full).
+template <class Table>
+__device__ __forceinline__ int register_key(Table& table, uint32_t key) {
+    const uint32_t full = 0xffffffffu;
+    uint32_t peers = __match_any_sync(full, key);
+    int leader = __ffs(peers) - 1;
+    int slot = -1;
+    if (static_cast<int>(lane_id()) == leader && key != kEmpty) slot = table.insert(key);
+    slot = __shfl_sync(full, slot, leader);
+    return key == kEmpty ? -1 : slot;
+}
+
+// Rotate an 8-entry register array left by r (0..7) with a 3-stage select network, so
+// element j of the result is element (j + r) & 7 of the input (static indices only).
+template <class T>
+__device__ __forceinline__ void rotate8(T (&a)[8], uint32_t r) {
+#pragma unroll
+    for (int b = 1; b <= 4; b <<= 1) {
+        bool on = (r & b) != 0;
+        T t[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) t[j] = on ? a[(j + b) & 7] : a[j];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = t[j];
+    }
+}
+
+// Shift an 8-entry register array down by one (element 7 keeps its value).
+template <class T>
+__device__ __forceinline__ void shift8(T (&a)[8]) {
+#pragma unroll
+    for (int j = 0; j < 7; ++j) a[j] = a[j + 1];
+}
+
+__device__ __forceinline__ uint32_t rotate_mask8(uint32_t m, uint32_t r) {
+    return ((m >> r) | (m << (8 - r))) & 0xffu;
+}
+
+// Per-lane rotation for 8x4 warp patches: lanes that share a rotation are spread apart.
+__device__ __forceinline__ uint32_t lane_rotation() {
+    uint32_t l = lane_id();
+    return (l + 3u * (l >> 3)) & 7u;
+}
+
+#ifdef __CUDACC__
+// Opt a kernel into more than 48 KB of dynamic shared memory (a no-op below that).
+template <class Kernel>
+inline cudaError_t allow_dynamic_smem(Kernel kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(bytes));
+}
+#endif
 
 }  // namespace sad

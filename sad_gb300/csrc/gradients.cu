@@ -1,6 +1,7 @@
 // gradients.cu -- fused training gradient: forward softmax, dL/dpred of the MSE (+ SSIM)
 // loss, per-site parameter gradients and the prune removal delta, accumulated per 16x16
-// tile in a shared-memory table with warp-merged inserts (accum.cuh).
+// tile in a shared-memory table (accum.cuh): float for API calls, 64-bit fixed point
+// (bitwise reproducible) for the trainer.
 //
 // Semantics follow backends/cuda/src/gradients.cu:103-486 (computeGradientsTiledKernel):
 //   * masked pixels (mask <= 0) contribute nothing (the reference returns before its
@@ -11,16 +12,19 @@
 //     over duplicate slots (gradients.cu:295-350).
 //
 // Tile mapping: 256 threads = 8 warps, each warp an 8x4 pixel patch, so the lanes of a
-// warp share most candidates and the warp merge collapses them before the shared table.
+// warp share most candidates and register each site with one CAS per warp.
 #include "accum.cuh"
 #include "common.cuh"
 #include "host_common.h"
 #include "kernels.h"
 #include "sources.cuh"
 
+#include <type_traits>
+
 namespace sad {
 
 constexpr int kGradSlots = 512;
+constexpr float kRemovalSentinel = 1.0e6f;  // removal delta of a pixel the site dominates
 
 __device__ __forceinline__ float luma(const float* __restrict__ p) {
     return __ldg(p) * 0.299f + __ldg(p + 1) * 0.587f + __ldg(p + 2) * 0.114f;
@@ -63,24 +67,58 @@ __device__ float ssim_dloss(const float* __restrict__ ren, const float* __restri
     return (dA * B + A * dB) / den - num * (dC * D + C * dD) / (den * den);
 }
 
-template <bool kAoS, int NV>
+// Global fallback: float SoA arrays (API, accumulated like the reference) or the trainer's
+// [N][12] fixed-point records (slot 10 = removal delta, 11 = sentinel count).
+template <bool kFix, int NV>
 __device__ __forceinline__ void global_add(const GradParams& p, uint32_t key, const float (&v)[NV]) {
-    if (kAoS) {
-        float* o = p.aos12 + static_cast<size_t>(key) * 12;
-        red_add_v4(o, v[0], v[1], v[2], v[3]);
-        red_add_v4(o + 4, v[4], v[5], v[6], v[7]);
-        red_add_v4(o + 8, v[8], v[9], NV > 10 ? v[NV > 10 ? 10 : 0] : 0.0f, 0.0f);
+    if constexpr (kFix) {
+        long long* o = p.fix12 + static_cast<size_t>(key) * 12;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) fix_add_global(o + k, to_fix(v[k]));
     } else {
 #pragma unroll
         for (int k = 0; k < 10; ++k) atomicAdd(p.soa[k] + key, v[k]);
-        if (NV > 10 && v[NV > 10 ? 10 : 0] != 0.0f) atomicAdd(p.removal + key, v[NV > 10 ? 10 : 0]);
+        if constexpr (NV > 10) {
+            if (v[10] != 0.0f) atomicAdd(p.removal + key, v[10]);
+        }
     }
 }
 
-template <class Src, bool kAoS, bool kRemoval, bool kSSIM>
-__global__ void __launch_bounds__(256) fused_gradients_kernel(GradParams prm, Src src) {
-    constexpr int NV = kRemoval ? 11 : 10;
-    __shared__ TileTable<NV, kGradSlots> table;
+template <bool kFix, int NV, class Table>
+__device__ __forceinline__ void flush_slot(const GradParams& p, const Table& table, int s) {
+    const uint32_t key = table.key_at(s);
+    if constexpr (kFix) {
+        long long* o = p.fix12 + static_cast<size_t>(key) * 12;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            long long v = table.fixed(k, s);
+            if (v != 0) fix_add_global(o + k, v);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 10; ++k) atomicAdd(p.soa[k] + key, table.value(k, s));
+        if constexpr (NV > 10) {
+            float r = table.value(10, s);
+            if (r != 0.0f) atomicAdd(p.removal + key, r);
+        }
+    }
+}
+
+// Values per table slot: 10 gradients, + removal delta (float path), + removal delta and
+// count of "keep < 1e-4" pixels (fixed-point path; each such pixel adds the reference's
+// 1e6 sentinel, kept as an exact integer count so the fixed-point sum cannot overflow).
+template <bool kFix, bool kRemoval>
+struct GradLayout {
+    static constexpr int NV = kRemoval ? (kFix ? 12 : 11) : 10;
+    using Mode = typename std::conditional<kFix, AccSplit, AccFloat>::type;
+    using Table = TileTable<NV, kGradSlots, Mode>;
+};
+
+template <class Src, bool kFix, bool kRemoval, bool kSSIM>
+__global__ void __launch_bounds__(256, 4) fused_gradients_kernel(GradParams prm, Src src) {
+    using L = GradLayout<kFix, kRemoval>;
+    constexpr int NV = L::NV;
+    auto& table = shared_table<typename L::Table>();
     const int tid = threadIdx.x;
     table.init(tid, 256);
     __syncthreads();
@@ -96,9 +134,9 @@ __global__ void __launch_bounds__(256) fused_gradients_kernel(GradParams prm, Sr
 
     uint32_t ids[kCand];
     float wts[kCand];
+    float rem[kCand];
     uint32_t valid = 0, blend = 0;
     float3 pred = make_float3(0.f, 0.f, 0.f), dLdp = make_float3(0.f, 0.f, 0.f);
-    float rem[kCand];
 #pragma unroll
     for (int i = 0; i < kCand; ++i) {
         ids[i] = kEmpty;
@@ -154,14 +192,14 @@ __global__ void __launch_bounds__(256) fused_gradients_kernel(GradParams prm, Sr
             float3 tgt = make_float3(__ldg(t), __ldg(t + 1), __ldg(t + 2));
             dLdp = make_float3(2.0f * (pred.x - tgt.x), 2.0f * (pred.y - tgt.y),
                                2.0f * (pred.z - tgt.z));
-            if (kSSIM) {
+            if constexpr (kSSIM) {
                 float ds = ssim_dloss(prm.rendered, prm.target, x, y, w, h);
                 float k = -prm.ssim_weight * ds;
                 dLdp.x += k * 0.299f;
                 dLdp.y += k * 0.587f;
                 dLdp.z += k * 0.114f;
             }
-            if (kRemoval) {
+            if constexpr (kRemoval) {
                 // first slot of each distinct valid site carries its removal delta
 #pragma unroll
                 for (int i = 0; i < kCand; ++i) {
@@ -178,7 +216,7 @@ __global__ void __launch_bounds__(256) fused_gradients_kernel(GradParams prm, Sr
                     float keep = 1.0f - wt;
                     float delta;
                     if (keep < 1e-4f) {
-                        delta = 1.0e6f;
+                        delta = kRemovalSentinel;
                     } else {
                         float3 c = cols[i];
                         float3 pk = make_float3((pred.x - wt * c.x) / keep, (pred.y - wt * c.y) / keep,
@@ -196,66 +234,101 @@ __global__ void __launch_bounds__(256) fused_gradients_kernel(GradParams prm, Sr
         }
     }
 
+    // 1. one CAS per (warp, site): register every candidate of the warp in the table
+    int slots[kCand];
 #pragma unroll
-    for (int i = 0; i < kCand; ++i) {
-        float v[NV];
-        uint32_t key = kEmpty;
-        if (valid >> i & 1u) {
+    for (int i = 0; i < kCand; ++i)
+        slots[i] = register_key(table, (valid >> i & 1u) ? ids[i] : kEmpty);
+
+    // 2. accumulate in a lane-rotated candidate order; the loop is kept rolled (the arrays
+    // shift down one entry per step) so the kernel body stays small in the instruction cache
+    const uint32_t r = lane_rotation();
+    rotate8(ids, r);
+    rotate8(wts, r);
+    rotate8(slots, r);
+    if constexpr (kRemoval) rotate8(rem, r);
+    uint32_t vr = rotate_mask8(valid, r);
+#pragma unroll 1
+    for (int j = 0; j < kCand; ++j) {
+        if (vr & 1u) {
             SiteGeom g;
             float3 col;
-            src.load(ids[i], g, col);
+            src.load(ids[0], g, col);
             float o[10];
-            candidate_grads(g, col, ux, uy, inv_s2, inv_scale, wts[i], dLdp, pred, true, o);
+            candidate_grads(g, col, ux, uy, inv_s2, inv_scale, wts[0], dLdp, pred, true, o);
+            float v[NV];
 #pragma unroll
             for (int k = 0; k < 10; ++k) v[k] = o[k];
-            if (NV > 10) v[NV - 1] = rem[i];
-            key = ids[i];
-        } else {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) v[k] = 0.0f;
+            if constexpr (kRemoval) {
+                if constexpr (kFix) {
+                    bool sentinel = rem[0] == kRemovalSentinel;
+                    v[10] = sentinel ? 0.0f : rem[0] * prm.removal_fix_mul;
+                    v[11] = sentinel ? kFixInvScale : 0.0f;  // adds exactly 1
+                } else {
+                    v[10] = rem[0];
+                }
+            }
+            if (slots[0] >= 0)
+                table.add(slots[0], v);
+            else
+                global_add<kFix, NV>(prm, ids[0], v);
         }
-        bool leader = warp_merge_by_key<NV>(key, v);
-        if (leader && key != kEmpty) {
-            if (!table.add(key, v)) global_add<kAoS, NV>(prm, key, v);
-        }
+        vr >>= 1;
+        shift8(ids);
+        shift8(wts);
+        shift8(slots);
+        if constexpr (kRemoval) shift8(rem);
     }
     __syncthreads();
-    for (int s = tid; s < kGradSlots; s += 256) {
-        uint32_t key = table.keys[s];
-        if (key == kEmpty) continue;
-        float v[NV];
-#pragma unroll
-        for (int k = 0; k < NV; ++k) v[k] = table.vals[k][s];
-        global_add<kAoS, NV>(prm, key, v);
-    }
+    const int used = table.size();
+    for (int d = tid; d < used; d += 256) flush_slot<kFix, NV>(prm, table, d);
 }
 
-template <class Src, bool kAoS>
-static void dispatch_gradients(const GradParams& p, Src src, cudaStream_t st) {
+template <class Src, bool kFix, bool kRemoval, bool kSSIM>
+static void launch_fused(const GradParams& p, Src src, cudaStream_t st) {
     dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
+    size_t smem = sizeof(typename GradLayout<kFix, kRemoval>::Table);
+    fused_gradients_kernel<Src, kFix, kRemoval, kSSIM><<<grid, 256, smem, st>>>(p, src);
+}
+
+template <class Src, bool kFix>
+static void dispatch_gradients(const GradParams& p, Src src, cudaStream_t st) {
     bool rem = p.compute_removal != 0;
     bool ssim = p.ssim_weight > 0.0f;
     if (rem && ssim)
-        fused_gradients_kernel<Src, kAoS, true, true><<<grid, 256, 0, st>>>(p, src);
+        launch_fused<Src, kFix, true, true>(p, src, st);
     else if (rem)
-        fused_gradients_kernel<Src, kAoS, true, false><<<grid, 256, 0, st>>>(p, src);
+        launch_fused<Src, kFix, true, false>(p, src, st);
     else if (ssim)
-        fused_gradients_kernel<Src, kAoS, false, true><<<grid, 256, 0, st>>>(p, src);
+        launch_fused<Src, kFix, false, true>(p, src, st);
     else
-        fused_gradients_kernel<Src, kAoS, false, false><<<grid, 256, 0, st>>>(p, src);
+        launch_fused<Src, kFix, false, false>(p, src, st);
     note_launches(1);
 }
 
+template <class Src, bool kFix, bool kRemoval>
+static cudaError_t allow_variant() {
+    size_t smem = sizeof(typename GradLayout<kFix, kRemoval>::Table);
+    cudaError_t e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false>, smem);
+    if (e != cudaSuccess) return e;
+    return allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true>, smem);
+}
+
+cudaError_t prepare_gradient_kernels() {
+    cudaError_t e = allow_variant<RawSites, false, true>();
+    if (e == cudaSuccess) e = allow_variant<PreparedSites, false, true>();
+    if (e == cudaSuccess) e = allow_variant<PreparedSites, true, false>();
+    if (e == cudaSuccess) e = allow_variant<PreparedSites, true, true>();
+    return e;
+}
+
 void launch_gradients_raw(const GradParams& p, const Site* sites, cudaStream_t st) {
-    if (p.aos12)
-        dispatch_gradients<RawSites, true>(p, RawSites{sites}, st);
-    else
-        dispatch_gradients<RawSites, false>(p, RawSites{sites}, st);
+    dispatch_gradients<RawSites, false>(p, RawSites{sites}, st);
 }
 
 void launch_gradients_prepared(const GradParams& p, const SiteGeom* geom, const SiteColor* color,
                                cudaStream_t st) {
-    if (p.aos12)
+    if (p.fix12)
         dispatch_gradients<PreparedSites, true>(p, PreparedSites{geom, color}, st);
     else
         dispatch_gradients<PreparedSites, false>(p, PreparedSites{geom, color}, st);
@@ -300,7 +373,7 @@ extern "C" sad_status_t sad_compute_gradients_tiled(
                     grad_color_g, grad_color_b, grad_dir_x, grad_dir_y, grad_log_aniso};
     for (int k = 0; k < 10; ++k) p.soa[k] = g[k];
     p.removal = removal_delta;
-    p.aos12 = nullptr;
+    p.fix12 = nullptr;
     p.compute_removal = compute_removal ? 1 : 0;
     launch_gradients_raw(p, reinterpret_cast<const Site*>(sites), as_stream(stream));
     return check_launch("sad_compute_gradients_tiled");

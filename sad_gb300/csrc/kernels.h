@@ -78,13 +78,17 @@ struct GradParams {
     uint32_t site_count;
     float ssim_weight;
     int width, height, cand_width, cand_height;
-    // outputs: either 10 SoA arrays (+ removal) or one [N][12] array (slot 10 = removal)
+    // outputs: either 10 float SoA arrays (+ removal), accumulated, or the trainer's [N][12]
+    // records of 64-bit fixed point (2^-32 units; slots 0-9 gradients, 10 removal delta)
     float* soa[10];
     float* removal;
-    float* aos12;
+    long long* fix12;
+    float removal_fix_mul;  // fixed-point path: removal delta pre-scale (power of two <= 1)
     int compute_removal;
 };
 void launch_gradients_raw(const GradParams& p, const Site* sites, cudaStream_t st);
+// Opts the >48 KB shared-memory variants in; call once per device before any capture.
+cudaError_t prepare_gradient_kernels();
 void launch_gradients_prepared(const GradParams& p, const SiteGeom* geom, const SiteColor* color,
                                cudaStream_t st);
 
@@ -92,21 +96,21 @@ void launch_gradients_prepared(const GradParams& p, const SiteGeom* geom, const 
 void launch_tau_diffuse_raw(const uint32_t* c0, const uint32_t* c1, const Site* sites,
                             const float* raw, const float* gin, float* gout, uint32_t n,
                             float lambda, int w, int h, int ds, cudaStream_t st);
-// trainer form: log-tau gradient read from aos12 slot 2 (raw and first input), lambda from
-// the iteration counter
+// trainer form: raw log-tau gradient = slot 2 of the fixed-point records; gin == nullptr
+// reads the neighbours from there too (first pass); lambda from state->iter
 void launch_tau_diffuse_train(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
-                              const float* aos12, const float* gin, int gin_stride, float* gout,
-                              uint32_t n, const DevState* state, int iterations, int w, int h,
-                              int ds, cudaStream_t st);
+                              const long long* fix12, const float* gin, float* gout, uint32_t n,
+                              const DevState* state, int iterations, int w, int h, int ds,
+                              cudaStream_t st);
 struct AdamHyper {
     float lr_pos, lr_tau, lr_radius, lr_color, lr_dir, lr_aniso;
     float beta1, beta2, eps;
 };
 void launch_adam_soa(Site* sites, float* adam, const float* const g[10], const AdamHyper& hp,
                      uint32_t t, uint32_t n, int w, int h, cudaStream_t st);
-// trainer form: reads aos12 grads (log-tau from tau_grad), zeroes slots 0-9, writes the
-// prepared records; t = state->iter + 1
-void launch_adam_train(Site* sites, float* adam, float* aos12, const float* tau_grad,
+// trainer form: reads the fixed-point gradient records (log-tau from tau_grad), zeroes
+// slots 0-9, writes the refreshed SiteGeom/SiteColor; t = state->iter + 1
+void launch_adam_train(Site* sites, float* adam, long long* fix12, const float* tau_grad,
                        SiteGeom* geom, SiteColor* color, const AdamHyper& hp,
                        const DevState* state, uint32_t n, int w, int h, cudaStream_t st);
 void launch_clear_f32(float* buf, size_t count, cudaStream_t st);
@@ -126,6 +130,10 @@ void launch_densify_pairs(const Site* sites, const float* mass, const float* ene
 void launch_prune_pairs(const Site* sites, const float* removal, int removal_stride,
                         uint32_t* pairs, uint32_t n, float delta_norm, uint32_t pair_count,
                         cudaStream_t st);
+// trainer form: removal delta from slots 10 (fixed point, pre-scaled by fix_mul) and 11
+// (count of 1e6 sentinels) of the gradient records, both cleared
+void launch_prune_pairs_fixed(const Site* sites, long long* fix12, float fix_mul, uint32_t* pairs,
+                              uint32_t n, float delta_norm, uint32_t pair_count, cudaStream_t st);
 void launch_write_indices(const uint32_t* pairs, uint32_t* idx, uint32_t k, cudaStream_t st);
 void launch_prune_by_index(Site* sites, const uint32_t* idx, uint32_t k, cudaStream_t st);
 // trainer form: prune the first prune_k[state->iter] entries of sorted pairs, also in geom
@@ -138,6 +146,14 @@ void launch_split(Site* sites, float* adam, const uint32_t* split_idx, uint32_t 
 void launch_site_stats(const uint32_t* c0, const uint32_t* c1, const float* target,
                        const float* mask, const Site* sites, float inv_s2, uint32_t n,
                        float* const out[8], int w, int h, int cw, int ch, cudaStream_t st);
+// trainer form: 64-bit fixed-point accumulation into fix ([8][stride], zero on entry, left
+// zeroed), converted into out[k][0..n) -- bitwise reproducible
+void launch_site_stats_fixed(const uint32_t* c0, const uint32_t* c1, const float* target,
+                             const float* mask, const Site* sites, float inv_s2, uint32_t n,
+                             long long* fix, size_t stride, float* const out[8], int w, int h,
+                             int cw, int ch, cudaStream_t st);
+// pre-scale of the removal delta in the trainer's fixed-point gradient records
+float removal_fix_mul(int w, int h);
 void launch_hilbert_pairs(const Site* sites, uint32_t* pairs, uint32_t n, uint32_t padded, int w,
                           int h, int bits, cudaStream_t st);
 void launch_hilbert_order(const uint32_t* pairs, uint32_t* order, uint32_t* pos, uint32_t n,

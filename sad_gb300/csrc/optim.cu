@@ -8,6 +8,7 @@
 //   * Adam: t = iter + 1 (sad_cuda.cu:2369-2380), fused with the gradient clear
 //     (adam.cu:183-209) and with the refresh of the prepared SiteGeom/SiteColor records
 //     the per-pixel kernels gather.
+#include "accum.cuh"
 #include "common.cuh"
 #include "host_common.h"
 #include "kernels.h"
@@ -17,14 +18,13 @@ namespace sad {
 // ---------------------------------------------------------------------------
 // tau diffusion (backends/cuda/src/tau_diffusion.cu:27-89)
 // ---------------------------------------------------------------------------
-template <class PosFn>
+template <class PosFn, class RawFn, class GinFn>
 __device__ __forceinline__ float tau_diffuse_one(uint32_t i, const uint4* __restrict__ c0,
                                                  const uint4* __restrict__ c1, PosFn pos,
-                                                 const float* __restrict__ raw, int raw_stride,
-                                                 const float* __restrict__ gin, int gin_stride,
-                                                 uint32_t n, float lambda, int w, int h, int ds) {
+                                                 RawFn raw, GinFn gin, uint32_t n, float lambda,
+                                                 int w, int h, int ds) {
     float2 sp = pos(i);
-    if (lambda <= 0.0f || sp.x < 0.0f) return gin[static_cast<size_t>(i) * gin_stride];
+    if (lambda <= 0.0f || sp.x < 0.0f) return gin(i);
     float inv = 1.0f / fmaxf(static_cast<float>(ds), 1.0f);
     int px = clampi(static_cast<int>(sp.x * inv + 0.5f), 0, w - 1);
     int py = clampi(static_cast<int>(sp.y * inv + 0.5f), 0, h - 1);
@@ -42,11 +42,11 @@ __device__ __forceinline__ float tau_diffuse_one(uint32_t i, const uint4* __rest
         for (int j = 0; j < k; ++j) seen |= ids[j] == m;
         if (seen) continue;
         if (pos(m).x < 0.0f) continue;
-        sum += gin[static_cast<size_t>(m) * gin_stride];
+        sum += gin(m);
         cnt += 1;
     }
     float diag = 1.0f + lambda * static_cast<float>(cnt);
-    return (raw[static_cast<size_t>(i) * raw_stride] + lambda * sum) / diag;
+    return (raw(i) + lambda * sum) / diag;
 }
 
 __global__ void tau_diffuse_raw_kernel(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
@@ -56,7 +56,9 @@ __global__ void tau_diffuse_raw_kernel(const uint4* __restrict__ c0, const uint4
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     auto pos = [sites](uint32_t k) { return make_float2(__ldg(&sites[k].px), __ldg(&sites[k].py)); };
-    gout[i] = tau_diffuse_one(i, c0, c1, pos, raw, 1, gin, 1, n, lambda, w, h, ds);
+    auto rawf = [raw](uint32_t k) { return raw[k]; };
+    auto ginf = [gin](uint32_t k) { return gin[k]; };
+    gout[i] = tau_diffuse_one(i, c0, c1, pos, rawf, ginf, n, lambda, w, h, ds);
 }
 
 void launch_tau_diffuse_raw(const uint32_t* c0, const uint32_t* c1, const Site* sites,
@@ -74,31 +76,41 @@ __device__ __forceinline__ float tau_lambda(uint32_t iter, int iterations) {
     return __fmul_rn(0.05f, __fadd_rn(0.1f, __fmul_rn(0.9f, blend)));
 }
 
+// Trainer form: the raw log-tau gradient is slot 2 of the fixed-point records; the first
+// pass also reads its neighbours from there (kFixGin), later passes from a float buffer.
+template <bool kFixGin>
 __global__ void tau_diffuse_train_kernel(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
                                          const SiteGeom* __restrict__ geom,
-                                         const float* __restrict__ aos12,
-                                         const float* __restrict__ gin, int gin_stride,
-                                         float* __restrict__ gout, uint32_t n,
-                                         const DevState* __restrict__ state, int iterations, int w,
-                                         int h, int ds) {
+                                         const long long* __restrict__ fix12,
+                                         const float* __restrict__ gin, float* __restrict__ gout,
+                                         uint32_t n, const DevState* __restrict__ state,
+                                         int iterations, int w, int h, int ds) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float lambda = tau_lambda(state->iter, iterations);
-    auto pos = [geom](uint32_t k) {
-        float2 v = __ldg(reinterpret_cast<const float2*>(geom + k));
-        return v;
-    };
-    gout[i] = tau_diffuse_one(i, c0, c1, pos, aos12 + 2, 12, gin, gin_stride, n, lambda, w, h, ds);
+    auto pos = [geom](uint32_t k) { return __ldg(reinterpret_cast<const float2*>(geom + k)); };
+    auto rawf = [fix12](uint32_t k) { return from_fix(fix12[static_cast<size_t>(k) * 12 + 2]); };
+    if constexpr (kFixGin) {
+        gout[i] = tau_diffuse_one(i, c0, c1, pos, rawf, rawf, n, lambda, w, h, ds);
+    } else {
+        auto ginf = [gin](uint32_t k) { return gin[k]; };
+        gout[i] = tau_diffuse_one(i, c0, c1, pos, rawf, ginf, n, lambda, w, h, ds);
+    }
 }
 
 void launch_tau_diffuse_train(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
-                              const float* aos12, const float* gin, int gin_stride, float* gout,
-                              uint32_t n, const DevState* state, int iterations, int w, int h,
-                              int ds, cudaStream_t st) {
+                              const long long* fix12, const float* gin, float* gout, uint32_t n,
+                              const DevState* state, int iterations, int w, int h, int ds,
+                              cudaStream_t st) {
     if (n == 0) return;
-    tau_diffuse_train_kernel<<<blocks_for(n, 256), 256, 0, st>>>(
-        reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), geom, aos12, gin,
-        gin_stride, gout, n, state, iterations, w, h, ds);
+    auto q0 = reinterpret_cast<const uint4*>(c0);
+    auto q1 = reinterpret_cast<const uint4*>(c1);
+    if (gin == nullptr)
+        tau_diffuse_train_kernel<true><<<blocks_for(n, 256), 256, 0, st>>>(
+            q0, q1, geom, fix12, nullptr, gout, n, state, iterations, w, h, ds);
+    else
+        tau_diffuse_train_kernel<false><<<blocks_for(n, 256), 256, 0, st>>>(
+            q0, q1, geom, fix12, gin, gout, n, state, iterations, w, h, ds);
     note_launches(1);
 }
 
@@ -249,22 +261,24 @@ void launch_adam_soa(Site* sites, float* adam, const float* const g[10], const A
 }
 
 __global__ void adam_train_kernel(Site* __restrict__ sites, float* __restrict__ adam,
-                                  float* __restrict__ aos12, const float* __restrict__ tau_grad,
+                                  long long* __restrict__ fix12, const float* __restrict__ tau_grad,
                                   SiteGeom* __restrict__ geom, SiteColor* __restrict__ color,
                                   AdamHyper hp, const DevState* __restrict__ state, uint32_t n,
                                   int w, int h) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float norm = 1.0f / static_cast<float>(w * h);
-    float4* gq = reinterpret_cast<float4*>(aos12 + static_cast<size_t>(i) * 12);
-    float4 g0 = gq[0], g1 = gq[1];
-    float2 g2 = *reinterpret_cast<float2*>(aos12 + static_cast<size_t>(i) * 12 + 8);
-    // consume and clear slots 0-9 (slot 10, the removal delta, is read by the prune step)
-    gq[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-    gq[1] = make_float4(0.f, 0.f, 0.f, 0.f);
-    *reinterpret_cast<float2*>(aos12 + static_cast<size_t>(i) * 12 + 8) = make_float2(0.f, 0.f);
-    float g[10] = {g0.x * norm, g0.y * norm, tau_grad[i] * norm, g0.w * norm, g1.x * norm,
-                   g1.y * norm, g1.z * norm, g1.w * norm, g2.x * norm, g2.y * norm};
+    longlong2* gq = reinterpret_cast<longlong2*>(fix12 + static_cast<size_t>(i) * 12);
+    longlong2 q[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) q[k] = gq[k];
+    // consume and clear slots 0-9 (slots 10-11, the removal delta, are read by the prune step)
+#pragma unroll
+    for (int k = 0; k < 5; ++k) gq[k] = make_longlong2(0, 0);
+    float g[10] = {from_fix(q[0].x) * norm, from_fix(q[0].y) * norm, tau_grad[i] * norm,
+                   from_fix(q[1].y) * norm, from_fix(q[2].x) * norm, from_fix(q[2].y) * norm,
+                   from_fix(q[3].x) * norm, from_fix(q[3].y) * norm, from_fix(q[4].x) * norm,
+                   from_fix(q[4].y) * norm};
     Site s = site_load(sites, i);
     if (s.px < 0.0f) return;
     float tt = static_cast<float>(state->iter + 1u);
@@ -279,11 +293,11 @@ __global__ void adam_train_kernel(Site* __restrict__ sites, float* __restrict__ 
     reinterpret_cast<float4*>(color)[i] = make_float4(s.r, s.g, s.b, 0.0f);
 }
 
-void launch_adam_train(Site* sites, float* adam, float* aos12, const float* tau_grad,
+void launch_adam_train(Site* sites, float* adam, long long* fix12, const float* tau_grad,
                        SiteGeom* geom, SiteColor* color, const AdamHyper& hp,
                        const DevState* state, uint32_t n, int w, int h, cudaStream_t st) {
     if (n == 0) return;
-    adam_train_kernel<<<blocks_for(n, 256), 256, 0, st>>>(sites, adam, aos12, tau_grad, geom, color,
+    adam_train_kernel<<<blocks_for(n, 256), 256, 0, st>>>(sites, adam, fix12, tau_grad, geom, color,
                                                           hp, state, n, w, h);
     note_launches(1);
 }

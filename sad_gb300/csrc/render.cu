@@ -182,7 +182,8 @@ __global__ void __launch_bounds__(256) render_backward_kernel(
     const uint4* __restrict__ cand0, const uint4* __restrict__ cand1,
     const float* __restrict__ grad_rgb, float* __restrict__ grad_sites, Src src, float inv_s2,
     uint32_t n, int w, int h, int cw, int ch) {
-    __shared__ TileTable<10, kBwdSlots> table;
+    using Table = TileTable<10, kBwdSlots, AccFloat>;
+    auto& table = shared_table<Table>();
     int tid = threadIdx.y * blockDim.x + threadIdx.x;
     table.init(tid, 256);
     __syncthreads();
@@ -198,6 +199,11 @@ __global__ void __launch_bounds__(256) render_backward_kernel(
     float3 dLdp = make_float3(0.f, 0.f, 0.f);
     uint32_t valid = 0;  // softmax members: id < n and !(position.x < 0)
     uint32_t blend = 0;  // colour contributors: position.x >= 0
+#pragma unroll
+    for (int i = 0; i < kCand; ++i) {
+        ids[i] = kEmpty;
+        wts[i] = 0.0f;
+    }
     if (inb) {
         int p = y * w + x;
         int ci = cand_index_for_pixel(x, y, w, h, cw, ch);
@@ -244,43 +250,45 @@ __global__ void __launch_bounds__(256) render_backward_kernel(
                                __ldg(grad_rgb + 3 * p + 2));
         }
     }
+    int slots[kCand];
 #pragma unroll
-    for (int i = 0; i < kCand; ++i) {
+    for (int i = 0; i < kCand; ++i)
+        slots[i] = register_key(table, (valid >> i & 1u) ? ids[i] : kEmpty);
+    const uint32_t r = lane_rotation();
+    rotate8(ids, r);
+    rotate8(wts, r);
+    rotate8(slots, r);
+    const uint32_t vr = rotate_mask8(valid, r);
+#pragma unroll
+    for (int j = 0; j < kCand; ++j) {
+        if (!(vr >> j & 1u)) continue;
+        SiteGeom g;
+        float3 col;
+        src.load(ids[j], g, col);
         float v[10];
-        uint32_t key = kEmpty;
-        if (valid >> i & 1u) {
-            SiteGeom g;
-            float3 col;
-            src.load(ids[i], g, col);
-            candidate_grads(g, col, ux, uy, inv_s2, inv_scale, wts[i], dLdp, pred, false, v);
-            key = ids[i];
+        candidate_grads(g, col, ux, uy, inv_s2, inv_scale, wts[j], dLdp, pred, false, v);
+        if (slots[j] >= 0) {
+            table.add(slots[j], v);
         } else {
+            float* gs = grad_sites + static_cast<size_t>(ids[j]) * 10;
 #pragma unroll
-            for (int k = 0; k < 10; ++k) v[k] = 0.0f;
-        }
-        bool leader = warp_merge_by_key<10>(key, v);
-        if (leader && key != kEmpty) {
-            if (!table.add(key, v)) {
-                float* gs = grad_sites + static_cast<size_t>(key) * 10;
-#pragma unroll
-                for (int k = 0; k < 10; ++k) atomicAdd(gs + k, v[k]);
-            }
+            for (int k = 0; k < 10; ++k) atomicAdd(gs + k, v[k]);
         }
     }
     __syncthreads();
-    for (int s = tid; s < kBwdSlots; s += 256) {
-        uint32_t key = table.keys[s];
-        if (key == kEmpty) continue;
-        float* gs = grad_sites + static_cast<size_t>(key) * 10;
+    const int used = table.size();
+    for (int d = tid; d < used; d += 256) {
+        float* gs = grad_sites + static_cast<size_t>(table.key_at(d)) * 10;
 #pragma unroll
-        for (int k = 0; k < 10; ++k) atomicAdd(gs + k, table.vals[k][s]);
+        for (int k = 0; k < 10; ++k) atomicAdd(gs + k, table.value(k, d));
     }
 }
 
 void launch_render_backward_raw(const uint32_t* c0, const uint32_t* c1, const float* grad_rgb,
                                 float* grad_sites, const Site* sites, float inv_s2, uint32_t n,
                                 int w, int h, int cw, int ch, cudaStream_t st) {
-    render_backward_kernel<RawSites><<<pixel_grid(w, h), dim3(32, 8), 0, st>>>(
+    render_backward_kernel<RawSites><<<pixel_grid(w, h), dim3(32, 8),
+                                       sizeof(TileTable<10, kBwdSlots, AccFloat>), st>>>(
         reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), grad_rgb,
         grad_sites, RawSites{sites}, inv_s2, n, w, h, cw, ch);
     note_launches(1);

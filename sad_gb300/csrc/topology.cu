@@ -5,6 +5,9 @@
 #include "common.cuh"
 #include "host_common.h"
 #include "kernels.h"
+
+#include <cmath>
+#include <type_traits>
 #include "sources.cuh"
 
 #include <vector>
@@ -66,6 +69,32 @@ void launch_prune_pairs(const Site* sites, const float* removal, int removal_str
     prune_pairs_kernel<<<blocks_for(pair_count, 256), 256, 0, st>>>(
         sites, const_cast<float*>(removal), removal_stride, removal_stride != 1,
         reinterpret_cast<uint2*>(pairs), n, delta_norm, pair_count);
+    note_launches(1);
+}
+
+__global__ void prune_pairs_fixed_kernel(const Site* __restrict__ sites, long long* __restrict__ fix12,
+                                         float inv_mul, uint2* __restrict__ pairs, uint32_t n,
+                                         float delta_norm, uint32_t pc) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pc) return;
+    uint2 o = make_uint2(kEmpty, kEmpty);
+    if (i < n) {
+        bool active = sites[i].px >= 0.0f;
+        longlong2* r = reinterpret_cast<longlong2*>(fix12 + static_cast<size_t>(i) * 12 + 10);
+        longlong2 v = *r;
+        *r = make_longlong2(0, 0);
+        float removal = static_cast<float>(v.y) * 1.0e6f + from_fix(v.x) * inv_mul;
+        float delta = removal * delta_norm;
+        if (active && isfinite(delta)) o = make_uint2(__float_as_uint(fmaxf(delta, 0.0f)), i);
+    }
+    pairs[i] = o;
+}
+
+void launch_prune_pairs_fixed(const Site* sites, long long* fix12, float fix_mul, uint32_t* pairs,
+                              uint32_t n, float delta_norm, uint32_t pair_count, cudaStream_t st) {
+    if (pair_count == 0) return;
+    prune_pairs_fixed_kernel<<<blocks_for(pair_count, 256), 256, 0, st>>>(
+        sites, fix12, 1.0f / fix_mul, reinterpret_cast<uint2*>(pairs), n, delta_norm, pair_count);
     note_launches(1);
 }
 
@@ -242,9 +271,15 @@ void launch_split(Site* sites, float* adam, const uint32_t* split_idx, uint32_t 
 // site statistics (backends/cuda/src/utils.cu:106-231)
 // ---------------------------------------------------------------------------
 struct StatOut {
-    float* o[8];
+    float* o[8];       // float path: accumulate into caller arrays
+    long long* fix;    // fixed-point path: [8][stride] records, 2^32 * mul[k] units
+    size_t stride;
+    float mul[8];      // per-statistic pre-scale (power of two <= 1), sized to the image
 };
 
+constexpr int kStatSlots = 512;
+
+template <bool kFix>
 __global__ void __launch_bounds__(256) site_stats_kernel(const uint4* __restrict__ c0,
                                                          const uint4* __restrict__ c1,
                                                          const float* __restrict__ target,
@@ -252,6 +287,12 @@ __global__ void __launch_bounds__(256) site_stats_kernel(const uint4* __restrict
                                                          RawSites src, float inv_s2, uint32_t n,
                                                          StatOut out, int w, int h, int cw,
                                                          int ch) {
+    using Table = TileTable<8, kStatSlots, typename std::conditional<kFix, AccSplit, AccFloat>::type>;
+    auto& table = shared_table<Table>();
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    table.init(tid, 256);
+    __syncthreads();
+
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     bool live = x < w && y < h;
@@ -314,11 +355,11 @@ __global__ void __launch_bounds__(256) site_stats_kernel(const uint4* __restrict
             err = d0 * d0 + d1 * d1 + d2 * d2;
         }
     }
-    // unique valid sites of the pixel, summed weight over duplicate slots
+    // unique valid sites of the pixel, each with its weight summed over duplicate slots
+    float wsum[kCand];
+    uint32_t uniq = 0;
 #pragma unroll
     for (int i = 0; i < kCand; ++i) {
-        float v[8];
-        uint32_t key = kEmpty;
         bool first = (valid >> i & 1u) != 0u;
 #pragma unroll
         for (int j = 0; j < i; ++j) first &= !((valid >> j & 1u) && ids[j] == ids[i]);
@@ -328,32 +369,114 @@ __global__ void __launch_bounds__(256) site_stats_kernel(const uint4* __restrict
             for (int j = i; j < kCand; ++j)
                 if ((valid >> j & 1u) && ids[j] == ids[i]) wt += wts[j];
         }
-        if (first && wt > 0.0f) {
-            float we = wt * fminf(err, 1.0f);
-            v[0] = wt; v[1] = wt * err; v[2] = we; v[3] = we * ux; v[4] = we * uy;
-            v[5] = we * ux * ux; v[6] = we * ux * uy; v[7] = we * uy * uy;
-            key = ids[i];
+        wsum[i] = wt;
+        if (first && wt > 0.0f) uniq |= 1u << i;
+    }
+    int slots[kCand];
+#pragma unroll
+    for (int i = 0; i < kCand; ++i)
+        slots[i] = register_key(table, (uniq >> i & 1u) ? ids[i] : kEmpty);
+    const uint32_t r = lane_rotation();
+    rotate8(ids, r);
+    rotate8(wsum, r);
+    rotate8(slots, r);
+    const uint32_t ur = rotate_mask8(uniq, r);
+    const float ef = fminf(err, 1.0f);
+#pragma unroll
+    for (int j = 0; j < kCand; ++j) {
+        if (!(ur >> j & 1u)) continue;
+        float wt = wsum[j];
+        float we = wt * ef;
+        float v[8] = {wt, wt * err, we, we * ux, we * uy, we * ux * ux, we * ux * uy, we * uy * uy};
+        if constexpr (kFix) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] *= out.mul[k];
+        }
+        if (slots[j] >= 0) {
+            table.add(slots[j], v);
         } else {
 #pragma unroll
-            for (int k = 0; k < 8; ++k) v[k] = 0.0f;
+            for (int k = 0; k < 8; ++k) {
+                if constexpr (kFix)
+                    fix_add_global(out.fix + k * out.stride + ids[j], to_fix(v[k]));
+                else
+                    atomicAdd(out.o[k] + ids[j], v[k]);
+            }
         }
-        bool leader = warp_merge_by_key<8>(key, v);
-        if (leader && key != kEmpty) {
+    }
+    __syncthreads();
+    const int used = table.size();
+    for (int s = tid; s < used; s += 256) {
+        const uint32_t key = table.key_at(s);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) atomicAdd(out.o[k] + key, v[k]);
+        for (int k = 0; k < 8; ++k) {
+            if constexpr (kFix) {
+                long long v = table.fixed(k, s);
+                if (v != 0) fix_add_global(out.fix + k * out.stride + key, v);
+            } else {
+                atomicAdd(out.o[k] + key, table.value(k, s));
+            }
         }
     }
 }
 
+// fixed-point statistics -> float arrays; clears the records for the next use
+__global__ void stats_finalize_kernel(StatOut out, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        long long* f = out.fix + k * out.stride + i;
+        out.o[k][i] = from_fix(*f) / out.mul[k];
+        *f = 0;
+    }
+}
+
+static dim3 stats_grid(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }
+
 void launch_site_stats(const uint32_t* c0, const uint32_t* c1, const float* target,
                        const float* mask, const Site* sites, float inv_s2, uint32_t n,
                        float* const out[8], int w, int h, int cw, int ch, cudaStream_t st) {
-    StatOut o;
+    StatOut o{};
     for (int k = 0; k < 8; ++k) o.o[k] = out[k];
-    site_stats_kernel<<<dim3((w + 31) / 32, (h + 7) / 8), dim3(32, 8), 0, st>>>(
+    site_stats_kernel<false><<<stats_grid(w, h), dim3(32, 8), sizeof(TileTable<8, kStatSlots, AccFloat>), st>>>(
         reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), target, mask,
         RawSites{sites}, inv_s2, n, o, w, h, cw, ch);
     note_launches(1);
+}
+
+// Power-of-two pre-scale (<= 1) keeping a fixed-point value exact: a tile's sum below
+// 2^23 (the split shared words, 256 pixel terms of at most per_pixel each) and a site's
+// total below 2^35 (the 64-bit record, npix terms).
+static float fix_mul_for_bound(double per_pixel, double npix) {
+    float mul = 1.0f;
+    while (mul > 0x1p-60f &&
+           (256.0 * per_pixel * mul >= 0x1p23 || npix * per_pixel * mul >= 0x1p35))
+        mul *= 0.5f;
+    return mul;
+}
+
+float removal_fix_mul(int w, int h) {
+    // per pixel |delta| <= 2^10 (squared colour errors of 3 channels)
+    return fix_mul_for_bound(1024.0, static_cast<double>(w) * h);
+}
+
+void launch_site_stats_fixed(const uint32_t* c0, const uint32_t* c1, const float* target,
+                             const float* mask, const Site* sites, float inv_s2, uint32_t n,
+                             long long* fix, size_t stride, float* const out[8], int w, int h,
+                             int cw, int ch, cudaStream_t st) {
+    StatOut o{};
+    for (int k = 0; k < 8; ++k) o.o[k] = out[k];
+    o.fix = fix;
+    o.stride = stride;
+    const double np = static_cast<double>(w) * h, fw = w, fh = h;
+    const double per_pixel[8] = {1.0, 1024.0, 1.0, fw, fh, fw * fw, fw * fh, fh * fh};
+    for (int k = 0; k < 8; ++k) o.mul[k] = fix_mul_for_bound(per_pixel[k], np);
+    site_stats_kernel<true><<<stats_grid(w, h), dim3(32, 8), sizeof(TileTable<8, kStatSlots, AccSplit>), st>>>(
+        reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), target, mask,
+        RawSites{sites}, inv_s2, n, o, w, h, cw, ch);
+    stats_finalize_kernel<<<blocks_for(n, 256), 256, 0, st>>>(o, n);
+    note_launches(2);
 }
 
 // ---------------------------------------------------------------------------

@@ -64,7 +64,9 @@ struct sad_trainer {
     sad::SiteColor* color = nullptr;
     sad::SiteGeom* vgeom = nullptr;
     float* adam = nullptr;
-    float* grads = nullptr;  // [cap][12]: 10 gradients, removal delta, pad
+    // [cap][12] 64-bit fixed-point records: 10 gradients, removal delta, sentinel count
+    long long* grads = nullptr;
+    float removal_mul = 1.0f;
     float* tau_a = nullptr;
     float* tau_b = nullptr;
     uint32_t* pairs = nullptr;
@@ -76,7 +78,8 @@ struct sad_trainer {
     uint32_t* hpos = nullptr;
     uint32_t* hpairs = nullptr;
     uint32_t hpadded = 0;
-    float* stats = nullptr;  // 8 x cap
+    float* stats = nullptr;         // 8 x cap
+    long long* stats_fix = nullptr;  // 8 x cap, zero between densify steps
     float* render = nullptr;
     float* metric = nullptr;
     uint32_t* count = nullptr;
@@ -239,7 +242,8 @@ static void launch_gradients_step(sad_trainer* t, int field, bool prune, cudaStr
     g.height = t->h;
     g.cand_width = t->cw;
     g.cand_height = t->ch;
-    g.aos12 = t->grads;
+    g.fix12 = t->grads;
+    g.removal_fix_mul = t->removal_mul;
     g.compute_removal = prune ? 1 : 0;
     launch_gradients_prepared(g, t->geom, t->color, s);
 }
@@ -267,15 +271,13 @@ static int iteration_body(sad_trainer* t, bool upd, bool prune, int field, int a
     }
     if (upd) cudaStreamWaitEvent(s, t->ev_join, 0);
     // 4 Jacobi passes: grads slot 2 -> A -> B -> A -> B
-    const float* gin = t->grads + 2;
-    int stride = 12;
+    const float* gin = nullptr;
     float* bufs[2] = {t->tau_a, t->tau_b};
     for (int pass = 0; pass < 4; ++pass) {
         float* out = bufs[pass & 1];
-        launch_tau_diffuse_train(t->cand0[next], t->cand1[next], t->geom, t->grads, gin, stride,
-                                 out, t->n, t->state, t->cfg.iterations, t->cw, t->ch, t->ds, s);
+        launch_tau_diffuse_train(t->cand0[next], t->cand1[next], t->geom, t->grads, gin, out,
+                                 t->n, t->state, t->cfg.iterations, t->cw, t->ch, t->ds, s);
         gin = out;
-        stride = 1;
     }
     AdamHyper hp{t->cfg.lr_pos * t->cfg.lr_scale, t->cfg.lr_tau * t->cfg.lr_scale,
                  t->cfg.lr_radius * t->cfg.lr_scale, t->cfg.lr_color * t->cfg.lr_scale,
@@ -285,7 +287,8 @@ static int iteration_body(sad_trainer* t, bool upd, bool prune, int field, int a
                       t->n, t->w, t->h, s);
     if (prune) {
         float delta_norm = 1.0f / std::max(1.0f, t->mask_sum);
-        launch_prune_pairs(t->sites, t->grads + 10, 12, t->pairs, t->n, delta_norm, t->cap, s);
+        launch_prune_pairs_fixed(t->sites, t->grads, t->removal_mul, t->pairs, t->n, delta_norm,
+                                 t->cap, s);
         launch_radix_sort(t->pairs, t->cap, 0xFFFFFFFFu, t->sort_temp, s);
         launch_prune_sorted_train(t->sites, t->geom, t->pairs, t->prune_k, t->state,
                                   SAD_MAX_SPLIT_INDICES, s);
@@ -298,10 +301,9 @@ static sad_status_t run_densify(sad_trainer* t, const IterPlan& p, cudaStream_t 
     // site statistics on the current field, score, sort, split (sad_cuda.cu:2232-2292)
     float* st[8];
     for (int k = 0; k < 8; ++k) st[k] = t->stats + static_cast<size_t>(k) * t->cap;
-    launch_clear_f32(t->stats, static_cast<size_t>(8) * t->cap, s);
-    launch_site_stats(t->cand0[t->cur], t->cand1[t->cur], t->target,
-                      t->have_mask ? t->mask : nullptr, t->sites, t->inv_s2, t->n, st, t->w, t->h,
-                      t->cw, t->ch, s);
+    launch_site_stats_fixed(t->cand0[t->cur], t->cand1[t->cur], t->target,
+                            t->have_mask ? t->mask : nullptr, t->sites, t->inv_s2, t->n,
+                            t->stats_fix, t->cap, st, t->w, t->h, t->cw, t->ch, s);
     launch_densify_pairs(t->sites, st[0], st[1], t->pairs, t->n, 1.0f, t->cfg.densify_score_alpha,
                          t->cap, s);
     launch_radix_sort(t->pairs, t->cap, 0xFFFFFFFFu, t->sort_temp, s);
@@ -421,6 +423,7 @@ extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int wi
     ALLOC(t->hpos, cap);
     ALLOC(t->hpairs, static_cast<size_t>(t->hpadded) * 2);
     ALLOC(t->stats, static_cast<size_t>(cap) * 8);
+    ALLOC(t->stats_fix, static_cast<size_t>(cap) * 8);
     ALLOC(t->render, np * 3);
     ALLOC(t->metric, 4);
     ALLOC(t->count, 4);
@@ -428,6 +431,8 @@ extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int wi
     ALLOC(t->prune_k, std::max(1, cfg->iterations));
 #undef ALLOC
     if (s == SAD_OK) s = dalloc(t, &t->sort_temp, sort_bytes);
+    if (s == SAD_OK) s = check_cuda(prepare_gradient_kernels(), "trainer kernel attributes");
+    t->removal_mul = removal_fix_mul(width, height);
     if (s == SAD_OK) s = dalloc(t, &t->init_temp, init_temp_bytes(static_cast<uint32_t>(cfg->n_sites)));
     if (s == SAD_OK)
         s = check_cuda(cudaStreamCreateWithFlags(&t->st, cudaStreamNonBlocking), "trainer stream");
@@ -552,7 +557,10 @@ extern "C" sad_status_t sad_trainer_init(sad_trainer_t* t, const float* sites_ho
     }
     launch_prepare_sites(t->sites, t->geom, t->color, t->cap, s);
     SAD_TRY(check_cuda(cudaMemsetAsync(t->adam, 0, static_cast<size_t>(t->cap) * 80, s), "trainer adam clear"));
-    SAD_TRY(check_cuda(cudaMemsetAsync(t->grads, 0, static_cast<size_t>(t->cap) * 48, s), "trainer grad clear"));
+    SAD_TRY(check_cuda(cudaMemsetAsync(t->grads, 0, static_cast<size_t>(t->cap) * 12 * sizeof(long long), s),
+                       "trainer grad clear"));
+    SAD_TRY(check_cuda(cudaMemsetAsync(t->stats_fix, 0, static_cast<size_t>(t->cap) * 8 * sizeof(long long), s),
+                       "trainer stats clear"));
     SAD_TRY(check_cuda(cudaMemsetAsync(t->state, 0, sizeof(DevState), s), "trainer state clear"));
     t->n = n0;
     t->active = active;

@@ -9,14 +9,16 @@ Tolerances (stated here, used below):
   * candidate lists from distance ranking: identical except where two distances agree to
     1e-5 relative (CPU libm expf / no-FMA vs CUDA), and identical lists on >= 99% pixels;
   * rendered RGB: max abs error <= 1e-4;
-  * per-site gradients: |gpu - oracle| <= 1e-3 * (sum over pixels of |term|) + 1e-6 per
-    component (the oracle sums in double; the GPU's float atomics have no fixed order).
+  * per-site gradients: relative L2 error per parameter <= 1e-3 and every entry within 5%
+    of its sum of absolute pixel terms (the oracle sums in double without FMA; the API
+    kernels sum with float atomics in no fixed order, like the reference).
 """
 import numpy as np
 import pytest
 import torch
 
 import cases
+from checks import assert_close_sum, assert_grads_close, assert_lists_match, packed_dist_np, raw_dist_np
 
 pytestmark = pytest.mark.gpu
 
@@ -40,63 +42,6 @@ def u32(t):
 def ops(cuda):
     from sad_gb300 import ops as _ops
     return _ops
-
-
-def packed_dist_np(sites, ids, xs, ys, inv_s2):
-    """Candidate distance of the VPT pass from f16-rounded site values (float64)."""
-    s = sites.astype(np.float16).astype(np.float64)
-    ok = ids < sites.shape[0]
-    i = np.where(ok, ids, 0)
-    g = s[i]
-    dx, dy = xs - g[..., 0], ys - g[..., 1]
-    proj = g[..., 7] * dx + g[..., 8] * dy
-    perp2 = np.maximum(dx * dx + dy * dy - proj * proj, 0)
-    l1 = np.exp(g[..., 9])
-    d2 = np.maximum((l1 * proj * proj + perp2 / l1) * inv_s2, 1e-8)
-    d = np.maximum(np.exp(g[..., 2]), 1e-4) * (np.sqrt(d2) - g[..., 3] * np.sqrt(inv_s2))
-    d = np.where(g[..., 0] < 0, np.inf, d)
-    return np.where(ok, d, np.inf)
-
-
-def raw_dist_np(sites, ids, xs, ys, inv_s2):
-    s = sites.astype(np.float64)
-    ok = ids < sites.shape[0]
-    g = s[np.where(ok, ids, 0)]
-    dx, dy = xs - g[..., 0], ys - g[..., 1]
-    proj = g[..., 7] * dx + g[..., 8] * dy
-    perp2 = np.maximum(dx * dx + dy * dy - proj * proj, 0)
-    l1 = np.exp(g[..., 9])
-    d2 = np.maximum((l1 * proj * proj + perp2 / l1) * inv_s2, 1e-8)
-    d = np.maximum(np.exp(g[..., 2]), 1e-4) * (np.sqrt(d2) - g[..., 3] * np.sqrt(inv_s2))
-    d = np.where(g[..., 0] < 0, np.inf, d)
-    return np.where(ok, d, np.inf)
-
-
-def assert_close_sum(got, want, absw, rtol=1e-3, atol=1e-6, what="gradient"):
-    """|got - want| <= rtol * absw + atol elementwise, reporting the worst violations."""
-    err = np.abs(got - want) - (rtol * absw + atol)
-    if np.any(err > 0):
-        idx = np.argsort(err.ravel())[::-1][:8]
-        rows = [(np.unravel_index(i, err.shape), float(got.ravel()[i]), float(want.ravel()[i]),
-                 float(absw.ravel()[i])) for i in idx if err.ravel()[i] > 0]
-        raise AssertionError(f"{what}: {int((err > 0).sum())} of {err.size} outside tolerance; "
-                             f"worst (index, got, want, abs-sum): {rows}")
-
-
-def assert_lists_match(got, want, dist_fn, w, h, min_exact=0.99):
-    """Tie-tolerant list comparison: lists may differ only where distances tie."""
-    got, want = got.reshape(w * h, -1), want.reshape(w * h, -1)
-    same = np.all(got == want, axis=1)
-    assert same.mean() >= min_exact, same.mean()
-    bad = np.nonzero(~same)[0]
-    if bad.size:
-        xs = (bad % w)[:, None].astype(np.float64)
-        ys = (bad // w)[:, None].astype(np.float64)
-        dg = np.sort(dist_fn(got[bad], xs, ys), axis=1)
-        dw = np.sort(dist_fn(want[bad], xs, ys), axis=1)
-        fin = np.isfinite(dg) & np.isfinite(dw)
-        assert np.array_equal(np.isfinite(dg), np.isfinite(dw))
-        assert np.all(np.abs(dg[fin] - dw[fin]) <= 1e-5 * np.maximum(np.abs(dw[fin]), 1e-3))
 
 
 # ---------------------------------------------------------------------------
@@ -140,7 +85,7 @@ def test_render_backward_matches_oracle(ops, orc, w, h, n, seed):
     got = ops.render_sad_backward(t32(c0), t32(c1), tf(sites), tf(gout), 1.0 / max(w, h) ** 2, w, h)
     want, absw = orc.render_backward(c0, c1, sites, gout, w, h)
     got = got.cpu().numpy().astype(np.float64)
-    assert_close_sum(got, want, absw)
+    assert_grads_close(got.T, want.T, absw.T)
 
 
 def test_autograd_function_and_fp64_finite_differences(cuda, orc):
@@ -166,7 +111,7 @@ def test_autograd_function_and_fp64_finite_differences(cuda, orc):
     assert worst < 2e-3, worst
     _, absw = orc.render_backward(c0, c1, sites, gout.astype(np.float32), w, h)
     g64 = orc.render_backward_d(c0, c1, s64, gout, w, h, inv_s2)
-    assert_close_sum(g, g64, absw)
+    assert_grads_close(g.T, g64.T, absw.T)
 
 
 # ---------------------------------------------------------------------------
@@ -285,7 +230,7 @@ def test_fused_gradients_match_oracle(ops, orc, w, h, n, removal, masked, ssim):
     g, a, rem = orc.compute_gradients(c0, c1, img, sites, w, h, mask=mask if masked else None,
                                       rendered=rendered, ssim_weight=ssim, removal=removal)
     got = np.stack([b.cpu().numpy() for b in bufs[:10]]).astype(np.float64)
-    assert_close_sum(got, g, a)
+    assert_grads_close(got, g, a)
     if removal:
         r = bufs[10].cpu().numpy().astype(np.float64)
         assert np.all(np.abs(r - rem) <= 1e-3 * np.maximum(np.abs(rem), 1.0) + 1e-4)
