@@ -25,14 +25,15 @@
 
 namespace sad {
 
-// Fixed point with 28 fractional bits (resolution 3.7e-9) in 64-bit global records
-// (range +-3.4e10 per site).
-constexpr int kFixFracBits = 28;
-constexpr float kFixScale = 268435456.0f;                 // 2^28
-constexpr float kFixInvScale = 3.7252902984619141e-09f;  // 2^-28
+// Fixed point with 24 fractional bits in 64-bit global records (range +-5.5e11 per site).
+// The resolution, 6e-8 per pixel term, is far below what Adam resolves: gradients are
+// divided by the pixel count and compared with eps = 1e-8.
+constexpr int kFixFracBits = 24;
+constexpr float kFixScale = 16777216.0f;                  // 2^24
+constexpr float kFixInvScale = 5.9604644775390625e-08f;  // 2^-24
 // Per tile, a fixed-point sum is kept as two 32-bit words (hi * 2^20 + lo): shared
 // memory has native 32-bit integer atomics but no native 64-bit add.  Exact while a tile's
-// sum of one value stays below 2^23 in magnitude (and each term below 2^23).
+// sum of one value stays below 2^27 in magnitude (and each term below 2^27).
 constexpr int kSplitLoBits = 20;
 
 __device__ __forceinline__ long long to_fix(float v) { return __float2ll_rn(v * kFixScale); }
@@ -49,22 +50,23 @@ __device__ __forceinline__ void fix_add_global(long long* p, long long v) {
 }
 
 // Split of to_fix(v) = h * 2^20 + l with |l| <= 2^19, in FP32 and INT32 arithmetic (a float
-// -> 64-bit integer conversion runs on the FP64 pipe).  With y = v * 2^8 (exact), adding
+// -> 64-bit integer conversion runs on the FP64 pipe).  With y = v * 2^4 (exact), adding
 // 1.5 * 2^23 rounds y to the nearest integer yr in the low mantissa bits; r = y - yr is exact
 // and |r| <= 1/2, and rounding r * 2^20 the same way gives l.  h * 2^20 + l is then
-// round-half-even(v * 2^28), the integer to_fix() gives for the global path.  h is 0 for
-// |v| < 2^-9.  |v| < 2^14 takes this path; larger terms (to 2^23) split exactly via F2I.
+// round-half-even(v * 2^24), the integer to_fix() gives for the global path.  h is 0 for
+// |v| < 2^-5.  |v| < 2^18 takes this path; larger terms (to 2^27) split exactly via F2I.
 __device__ __forceinline__ void split_fix(float v, int& h, int& l) {
     const float kMagic = 12582912.0f;  // 1.5 * 2^23
     const int kMagicBits = 0x4B400000;
-    if (fabsf(v) < 16384.0f) {
-        float y = v * 256.0f;
+    constexpr float kY = static_cast<float>(1 << (kFixFracBits - kSplitLoBits));
+    if (fabsf(v) < 262144.0f) {
+        float y = v * kY;
         float ym = y + kMagic;
         float r = y - (ym - kMagic);
         h = __float_as_int(ym) - kMagicBits;
         l = __float_as_int(fmaf(r, 1048576.0f, kMagic)) - kMagicBits;
     } else {
-        float y = v * 256.0f;  // an integer for |v| >= 2^15; otherwise split its fraction
+        float y = v * kY;  // at most one fractional bit; split it off
         float yf = truncf(y);
         h = __float2int_rz(yf);
         l = __float2int_rn((y - yf) * 1048576.0f);
@@ -153,8 +155,8 @@ struct TileTable<NV, SLOTS, AccFloat> : KeyTable<SLOTS> {
 };
 
 // Fixed-point words: x = to_fix(v) = hi * 2^20 + lo with |lo| <= 2^19, so the lo sum of
-// up to 2^11 terms fits an int32 and hi (zero for |v| < 2^-9, then skipped) wraps modulo
-// 2^32, which the recombination absorbs while the tile's total stays below 2^23.
+// up to 2^11 terms fits an int32 and hi (zero for |v| < 2^-5, then skipped) wraps modulo
+// 2^32, which the recombination absorbs while the tile's total stays below 2^27.
 template <int NV, int SLOTS>
 struct TileTable<NV, SLOTS, AccSplit> : KeyTable<SLOTS> {
     int hi[NV][SLOTS];

@@ -19,6 +19,7 @@
 #include "kernels.h"
 #include "sources.cuh"
 
+#include <atomic>
 #include <type_traits>
 
 namespace sad {
@@ -115,7 +116,7 @@ struct GradLayout {
 };
 
 template <class Src, bool kFix, bool kRemoval, bool kSSIM>
-__global__ void __launch_bounds__(256, 4) fused_gradients_kernel(GradParams prm, Src src) {
+__global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm, Src src) {
     using L = GradLayout<kFix, kRemoval>;
     constexpr int NV = L::NV;
     auto& table = shared_table<typename L::Table>();
@@ -291,8 +292,22 @@ static void launch_fused(const GradParams& p, Src src, cudaStream_t st) {
     fused_gradients_kernel<Src, kFix, kRemoval, kSSIM><<<grid, 256, smem, st>>>(p, src);
 }
 
+cudaError_t prepare_gradient_kernels();
+
+// Opt-in of the >48 KB shared-memory launches, once per device (an attribute set, not a
+// stream operation).
+static void ensure_gradient_kernels() {
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    if (prepare_gradient_kernels() == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+}
+
 template <class Src, bool kFix>
 static void dispatch_gradients(const GradParams& p, Src src, cudaStream_t st) {
+    ensure_gradient_kernels();
     bool rem = p.compute_removal != 0;
     bool ssim = p.ssim_weight > 0.0f;
     if (rem && ssim)

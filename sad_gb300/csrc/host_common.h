@@ -50,6 +50,7 @@ inline unsigned blocks_for(size_t n, unsigned threads) {
 // Counts kernel launches issued by this library (read by the benchmark to report how
 // many of its own kernels ran in a timed region).
 void note_launches(uint64_t n);
+void unnote_launches(uint64_t n);
 
 }  // namespace sad
 

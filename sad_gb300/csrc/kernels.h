@@ -96,23 +96,30 @@ void launch_gradients_prepared(const GradParams& p, const SiteGeom* geom, const 
 void launch_tau_diffuse_raw(const uint32_t* c0, const uint32_t* c1, const Site* sites,
                             const float* raw, const float* gin, float* gout, uint32_t n,
                             float lambda, int w, int h, int ds, cudaStream_t st);
-// trainer form: raw log-tau gradient = slot 2 of the fixed-point records; gin == nullptr
-// reads the neighbours from there too (first pass); lambda from state->iter
-void launch_tau_diffuse_train(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
-                              const long long* fix12, const float* gin, float* gout, uint32_t n,
-                              const DevState* state, int iterations, int w, int h, int ds,
-                              cudaStream_t st);
+// trainer form, first Jacobi pass: raw log-tau gradient from slot 2 of the fixed-point
+// records; records each active site's neighbour list nbr[n][8], raw[n] and active[n]
+void launch_tau_first_pass(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
+                           const long long* fix12, uint32_t* nbr, float* raw, uint8_t* active,
+                           float* gout, uint32_t n, const DevState* state, int iterations, int w,
+                           int h, int ds, cudaStream_t st);
+// trainer form, middle passes from the recorded lists
+void launch_tau_list_pass(const uint32_t* nbr, const float* raw, const uint8_t* active,
+                          const float* gin, float* gout, uint32_t n, const DevState* state,
+                          int iterations, cudaStream_t st);
 struct AdamHyper {
     float lr_pos, lr_tau, lr_radius, lr_color, lr_dir, lr_aniso;
     float beta1, beta2, eps;
 };
 void launch_adam_soa(Site* sites, float* adam, const float* const g[10], const AdamHyper& hp,
                      uint32_t t, uint32_t n, int w, int h, cudaStream_t st);
-// trainer form: reads the fixed-point gradient records (log-tau from tau_grad), zeroes
-// slots 0-9, writes the refreshed SiteGeom/SiteColor; t = state->iter + 1
-void launch_adam_train(Site* sites, float* adam, long long* fix12, const float* tau_grad,
+// trainer form: last tau pass (from tau_gin and the lists) fused with Adam on the
+// fixed-point records (slots 0-9 consumed and zeroed), refreshing SiteGeom/SiteColor;
+// t = state->iter + 1; inactive sites untouched
+void launch_adam_train(Site* sites, float* adam, long long* fix12, const uint32_t* nbr,
+                       const float* raw, const uint8_t* active, const float* tau_gin,
                        SiteGeom* geom, SiteColor* color, const AdamHyper& hp,
-                       const DevState* state, uint32_t n, int w, int h, cudaStream_t st);
+                       const DevState* state, int iterations, uint32_t n, int w, int h,
+                       cudaStream_t st);
 void launch_clear_f32(float* buf, size_t count, cudaStream_t st);
 void launch_advance_state(DevState* state, uint32_t vpt_passes, cudaStream_t st);
 
@@ -160,6 +167,9 @@ void launch_hilbert_order(const uint32_t* pairs, uint32_t* order, uint32_t* pos,
                           cudaStream_t st);
 void launch_mse(const float* ren, const float* tgt, const float* mask, float* acc, int w, int h,
                 cudaStream_t st);
+// reproducible form: fixed-point (2^-24) sum into *acc
+void launch_mse_fixed(const float* ren, const float* tgt, const float* mask, long long* acc, int w,
+                      int h, cudaStream_t st);
 void launch_ssim(const float* ren, const float* tgt, const float* mask, float* acc, int w, int h,
                  cudaStream_t st);
 void launch_count_active(const Site* sites, uint32_t* count, uint32_t n, cudaStream_t st);

@@ -24,6 +24,7 @@ void set_error(const char* fmt, ...) {
 void clear_error() { g_err[0] = '\0'; }
 
 void note_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void unnote_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
 }  // namespace sad
 

@@ -76,41 +76,111 @@ __device__ __forceinline__ float tau_lambda(uint32_t iter, int iterations) {
     return __fmul_rn(0.05f, __fadd_rn(0.1f, __fmul_rn(0.9f, blend)));
 }
 
-// Trainer form: the raw log-tau gradient is slot 2 of the fixed-point records; the first
-// pass also reads its neighbours from there (kFixGin), later passes from a float buffer.
-template <bool kFixGin>
-__global__ void tau_diffuse_train_kernel(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
-                                         const SiteGeom* __restrict__ geom,
-                                         const long long* __restrict__ fix12,
-                                         const float* __restrict__ gin, float* __restrict__ gout,
-                                         uint32_t n, const DevState* __restrict__ state,
-                                         int iterations, int w, int h, int ds) {
+// Trainer form.  The four Jacobi passes of an iteration share one candidate field and one
+// set of positions, so the first pass records each active site's neighbour list (the
+// distinct active candidates at its texel, in candidate order) and the raw gradient as a
+// float; the middle passes read the list; the last pass runs inside the Adam kernel.
+// Inactive sites are skipped: their diffused value is never read (a neighbour must be
+// active, and Adam skips inactive sites).
+struct TauLists {
+    uint4* nbr;        // [n][2] neighbour ids, kEmpty-padded
+    float* raw;        // [n] raw log-tau gradient (float)
+    uint8_t* active;   // [n] 1 = active site
+};
+
+__global__ void tau_first_pass_kernel(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
+                                      const SiteGeom* __restrict__ geom,
+                                      const long long* __restrict__ fix12, TauLists tl,
+                                      float* __restrict__ gout, uint32_t n,
+                                      const DevState* __restrict__ state, int iterations, int w,
+                                      int h, int ds) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float lambda = tau_lambda(state->iter, iterations);
-    auto pos = [geom](uint32_t k) { return __ldg(reinterpret_cast<const float2*>(geom + k)); };
-    auto rawf = [fix12](uint32_t k) { return from_fix(fix12[static_cast<size_t>(k) * 12 + 2]); };
-    if constexpr (kFixGin) {
-        gout[i] = tau_diffuse_one(i, c0, c1, pos, rawf, rawf, n, lambda, w, h, ds);
-    } else {
-        auto ginf = [gin](uint32_t k) { return gin[k]; };
-        gout[i] = tau_diffuse_one(i, c0, c1, pos, rawf, ginf, n, lambda, w, h, ds);
+    float2 sp = __ldg(reinterpret_cast<const float2*>(geom + i));
+    bool act = sp.x >= 0.0f;
+    tl.active[i] = act ? 1 : 0;
+    if (!act) return;
+    const float lambda = tau_lambda(state->iter, iterations);
+    const float r = from_fix(fix12[static_cast<size_t>(i) * 12 + 2]);
+    tl.raw[i] = r;
+    float inv = 1.0f / fmaxf(static_cast<float>(ds), 1.0f);
+    int px = clampi(static_cast<int>(sp.x * inv + 0.5f), 0, w - 1);
+    int py = clampi(static_cast<int>(sp.y * inv + 0.5f), 0, h - 1);
+    int p = py * w + px;
+    uint4 a = __ldg(c0 + p), b = __ldg(c1 + p);
+    uint32_t ids[kCand] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    uint32_t list[kCand];
+    float sum = 0.0f;
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kCand; ++k) {
+        list[k] = kEmpty;
+        uint32_t m = ids[k];
+        bool take = m < n && m != i;
+#pragma unroll
+        for (int j = 0; j < k; ++j) take &= ids[j] != m;
+        if (take) take = __ldg(&geom[m].px) >= 0.0f;
+        if (take) {
+            sum += from_fix(fix12[static_cast<size_t>(m) * 12 + 2]);
+            list[k] = m;
+            cnt += 1;
+        }
     }
+    tl.nbr[2 * i] = make_uint4(list[0], list[1], list[2], list[3]);
+    tl.nbr[2 * i + 1] = make_uint4(list[4], list[5], list[6], list[7]);
+    if (!(lambda > 0.0f)) {
+        gout[i] = r;
+        return;
+    }
+    gout[i] = (r + lambda * sum) / (1.0f + lambda * static_cast<float>(cnt));
 }
 
-void launch_tau_diffuse_train(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
-                              const long long* fix12, const float* gin, float* gout, uint32_t n,
-                              const DevState* state, int iterations, int w, int h, int ds,
-                              cudaStream_t st) {
+// One Jacobi pass of an active site from its recorded neighbour list (sum in candidate
+// order, as the first pass and the reference's kernel).
+__device__ __forceinline__ float tau_list_pass(const TauLists& tl, const float* __restrict__ gin,
+                                               uint32_t i, float lambda) {
+    const float r = tl.raw[i];
+    if (!(lambda > 0.0f)) return gin[i];
+    uint4 a = tl.nbr[2 * i], b = tl.nbr[2 * i + 1];
+    uint32_t ids[kCand] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    float sum = 0.0f;
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kCand; ++k) {
+        if (ids[k] == kEmpty) continue;
+        sum += gin[ids[k]];
+        cnt += 1;
+    }
+    return (r + lambda * sum) / (1.0f + lambda * static_cast<float>(cnt));
+}
+
+__global__ void tau_list_pass_kernel(TauLists tl, const float* __restrict__ gin,
+                                     float* __restrict__ gout, uint32_t n,
+                                     const DevState* __restrict__ state, int iterations) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !tl.active[i]) return;
+    gout[i] = tau_list_pass(tl, gin, i, tau_lambda(state->iter, iterations));
+}
+
+void launch_tau_first_pass(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
+                           const long long* fix12, uint32_t* nbr, float* raw, uint8_t* active,
+                           float* gout, uint32_t n, const DevState* state, int iterations, int w,
+                           int h, int ds, cudaStream_t st) {
     if (n == 0) return;
-    auto q0 = reinterpret_cast<const uint4*>(c0);
-    auto q1 = reinterpret_cast<const uint4*>(c1);
-    if (gin == nullptr)
-        tau_diffuse_train_kernel<true><<<blocks_for(n, 256), 256, 0, st>>>(
-            q0, q1, geom, fix12, nullptr, gout, n, state, iterations, w, h, ds);
-    else
-        tau_diffuse_train_kernel<false><<<blocks_for(n, 256), 256, 0, st>>>(
-            q0, q1, geom, fix12, gin, gout, n, state, iterations, w, h, ds);
+    TauLists tl{reinterpret_cast<uint4*>(nbr), raw, active};
+    tau_first_pass_kernel<<<blocks_for(n, 256), 256, 0, st>>>(
+        reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), geom, fix12, tl,
+        gout, n, state, iterations, w, h, ds);
+    note_launches(1);
+}
+
+void launch_tau_list_pass(const uint32_t* nbr, const float* raw, const uint8_t* active,
+                          const float* gin, float* gout, uint32_t n, const DevState* state,
+                          int iterations, cudaStream_t st) {
+    if (n == 0) return;
+    TauLists tl{reinterpret_cast<uint4*>(const_cast<uint32_t*>(nbr)), const_cast<float*>(raw),
+                const_cast<uint8_t*>(active)};
+    tau_list_pass_kernel<<<blocks_for(n, 256), 256, 0, st>>>(tl, gin, gout, n, state, iterations);
     note_launches(1);
 }
 
@@ -260,27 +330,31 @@ void launch_adam_soa(Site* sites, float* adam, const float* const g[10], const A
     note_launches(1);
 }
 
+// Trainer form: the last tau Jacobi pass, then Adam on the fixed-point gradient records,
+// which are consumed and cleared (slots 0-9; slots 10-11, the removal delta, belong to the
+// prune step), then the refreshed SiteGeom / SiteColor records.  Inactive sites carry no
+// gradient and are left untouched.
 __global__ void adam_train_kernel(Site* __restrict__ sites, float* __restrict__ adam,
-                                  long long* __restrict__ fix12, const float* __restrict__ tau_grad,
-                                  SiteGeom* __restrict__ geom, SiteColor* __restrict__ color,
-                                  AdamHyper hp, const DevState* __restrict__ state, uint32_t n,
+                                  long long* __restrict__ fix12, TauLists tl,
+                                  const float* __restrict__ tau_gin, SiteGeom* __restrict__ geom,
+                                  SiteColor* __restrict__ color, AdamHyper hp,
+                                  const DevState* __restrict__ state, int iterations, uint32_t n,
                                   int w, int h) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= n || !tl.active[i]) return;
+    const float tau_g = tau_list_pass(tl, tau_gin, i, tau_lambda(state->iter, iterations));
     float norm = 1.0f / static_cast<float>(w * h);
     longlong2* gq = reinterpret_cast<longlong2*>(fix12 + static_cast<size_t>(i) * 12);
     longlong2 q[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) q[k] = gq[k];
-    // consume and clear slots 0-9 (slots 10-11, the removal delta, are read by the prune step)
 #pragma unroll
     for (int k = 0; k < 5; ++k) gq[k] = make_longlong2(0, 0);
-    float g[10] = {from_fix(q[0].x) * norm, from_fix(q[0].y) * norm, tau_grad[i] * norm,
+    float g[10] = {from_fix(q[0].x) * norm, from_fix(q[0].y) * norm, tau_g * norm,
                    from_fix(q[1].y) * norm, from_fix(q[2].x) * norm, from_fix(q[2].y) * norm,
                    from_fix(q[3].x) * norm, from_fix(q[3].y) * norm, from_fix(q[4].x) * norm,
                    from_fix(q[4].y) * norm};
     Site s = site_load(sites, i);
-    if (s.px < 0.0f) return;
     float tt = static_cast<float>(state->iter + 1u);
     float c1 = 1.0f / (1.0f - powf(hp.beta1, tt));
     float c2 = 1.0f / (1.0f - powf(hp.beta2, tt));
@@ -293,12 +367,16 @@ __global__ void adam_train_kernel(Site* __restrict__ sites, float* __restrict__ 
     reinterpret_cast<float4*>(color)[i] = make_float4(s.r, s.g, s.b, 0.0f);
 }
 
-void launch_adam_train(Site* sites, float* adam, long long* fix12, const float* tau_grad,
+void launch_adam_train(Site* sites, float* adam, long long* fix12, const uint32_t* nbr,
+                       const float* raw, const uint8_t* active, const float* tau_gin,
                        SiteGeom* geom, SiteColor* color, const AdamHyper& hp,
-                       const DevState* state, uint32_t n, int w, int h, cudaStream_t st) {
+                       const DevState* state, int iterations, uint32_t n, int w, int h,
+                       cudaStream_t st) {
     if (n == 0) return;
-    adam_train_kernel<<<blocks_for(n, 256), 256, 0, st>>>(sites, adam, fix12, tau_grad, geom, color,
-                                                          hp, state, n, w, h);
+    TauLists tl{reinterpret_cast<uint4*>(const_cast<uint32_t*>(nbr)), const_cast<float*>(raw),
+                const_cast<uint8_t*>(active)};
+    adam_train_kernel<<<blocks_for(n, 256), 256, 0, st>>>(sites, adam, fix12, tl, tau_gin, geom,
+                                                          color, hp, state, iterations, n, w, h);
     note_launches(1);
 }
 

@@ -446,12 +446,12 @@ void launch_site_stats(const uint32_t* c0, const uint32_t* c1, const float* targ
 }
 
 // Power-of-two pre-scale (<= 1) keeping a fixed-point value exact: a tile's sum below
-// 2^23 (the split shared words, 256 pixel terms of at most per_pixel each) and a site's
-// total below 2^35 (the 64-bit record, npix terms).
+// 2^27 (the split shared words, 256 pixel terms of at most per_pixel each) and a site's
+// total below 2^39 (the 64-bit record, npix terms).
 static float fix_mul_for_bound(double per_pixel, double npix) {
     float mul = 1.0f;
     while (mul > 0x1p-60f &&
-           (256.0 * per_pixel * mul >= 0x1p23 || npix * per_pixel * mul >= 0x1p35))
+           (256.0 * per_pixel * mul >= 0x1p27 || npix * per_pixel * mul >= 0x1p39))
         mul *= 0.5f;
     return mul;
 }
@@ -578,6 +578,31 @@ __global__ void mse_kernel(const float* __restrict__ ren, const float* __restric
 void launch_mse(const float* ren, const float* tgt, const float* mask, float* acc, int w, int h,
                 cudaStream_t st) {
     mse_kernel<<<dim3((w + 31) / 32, (h + 7) / 8), dim3(32, 8), 0, st>>>(ren, tgt, mask, acc, w, h);
+    note_launches(1);
+}
+
+// Reproducible form: each block's sum (fixed order) added as a fixed-point integer.
+__global__ void mse_fixed_kernel(const float* __restrict__ ren, const float* __restrict__ tgt,
+                                 const float* __restrict__ mask, long long* __restrict__ acc, int w,
+                                 int h) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    float v = 0.0f;
+    if (x < w && y < h) {
+        int p = y * w + x;
+        if (!mask || mask[p] > 0.0f) {
+            float d0 = ren[3 * p] - tgt[3 * p], d1 = ren[3 * p + 1] - tgt[3 * p + 1],
+                  d2 = ren[3 * p + 2] - tgt[3 * p + 2];
+            v = d0 * d0 + d1 * d1 + d2 * d2;
+        }
+    }
+    float s = block_sum(v);
+    if (threadIdx.x == 0 && threadIdx.y == 0) fix_add_global(acc, to_fix(s));
+}
+
+void launch_mse_fixed(const float* ren, const float* tgt, const float* mask, long long* acc, int w,
+                      int h, cudaStream_t st) {
+    mse_fixed_kernel<<<dim3((w + 31) / 32, (h + 7) / 8), dim3(32, 8), 0, st>>>(ren, tgt, mask, acc, w, h);
     note_launches(1);
 }
 

@@ -27,6 +27,7 @@
 #include <cstring>
 #include <vector>
 
+#include "accum.cuh"
 #include "common.cuh"
 #include "host_common.h"
 #include "kernels.h"
@@ -69,6 +70,9 @@ struct sad_trainer {
     float removal_mul = 1.0f;
     float* tau_a = nullptr;
     float* tau_b = nullptr;
+    uint32_t* tau_nbr = nullptr;  // [cap][8] neighbour lists of the tau passes
+    float* tau_raw = nullptr;
+    uint8_t* tau_active = nullptr;
     uint32_t* pairs = nullptr;
     void* sort_temp = nullptr;
     uint32_t* idx = nullptr;
@@ -81,7 +85,7 @@ struct sad_trainer {
     float* stats = nullptr;         // 8 x cap
     long long* stats_fix = nullptr;  // 8 x cap, zero between densify steps
     float* render = nullptr;
-    float* metric = nullptr;
+    long long* metric = nullptr;  // fixed-point squared-error sum (reproducible PSNR)
     uint32_t* count = nullptr;
     sad::DevState* state = nullptr;
     uint32_t* prune_k = nullptr;
@@ -91,6 +95,7 @@ struct sad_trainer {
     cudaStream_t st = nullptr, side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaGraphExec_t graphs[2][2][3] = {};
+    uint64_t graph_kernels[2][2][3] = {};  // kernel launches one replay runs
     bool timing = false;
     std::vector<cudaEvent_t> tev;
     size_t tev_used = 0;
@@ -270,21 +275,20 @@ static int iteration_body(sad_trainer* t, bool upd, bool prune, int field, int a
         t->tev_used += 2;
     }
     if (upd) cudaStreamWaitEvent(s, t->ev_join, 0);
-    // 4 Jacobi passes: grads slot 2 -> A -> B -> A -> B
-    const float* gin = nullptr;
-    float* bufs[2] = {t->tau_a, t->tau_b};
-    for (int pass = 0; pass < 4; ++pass) {
-        float* out = bufs[pass & 1];
-        launch_tau_diffuse_train(t->cand0[next], t->cand1[next], t->geom, t->grads, gin, out,
-                                 t->n, t->state, t->cfg.iterations, t->cw, t->ch, t->ds, s);
-        gin = out;
-    }
+    // 4 Jacobi passes: grads slot 2 -> A -> B -> A -> (inside Adam)
+    launch_tau_first_pass(t->cand0[next], t->cand1[next], t->geom, t->grads, t->tau_nbr, t->tau_raw,
+                          t->tau_active, t->tau_a, t->n, t->state, t->cfg.iterations, t->cw, t->ch,
+                          t->ds, s);
+    launch_tau_list_pass(t->tau_nbr, t->tau_raw, t->tau_active, t->tau_a, t->tau_b, t->n, t->state,
+                         t->cfg.iterations, s);
+    launch_tau_list_pass(t->tau_nbr, t->tau_raw, t->tau_active, t->tau_b, t->tau_a, t->n, t->state,
+                         t->cfg.iterations, s);
     AdamHyper hp{t->cfg.lr_pos * t->cfg.lr_scale, t->cfg.lr_tau * t->cfg.lr_scale,
                  t->cfg.lr_radius * t->cfg.lr_scale, t->cfg.lr_color * t->cfg.lr_scale,
                  t->cfg.lr_dir * t->cfg.lr_scale, t->cfg.lr_aniso * t->cfg.lr_scale,
                  t->cfg.beta1, t->cfg.beta2, t->cfg.eps};
-    launch_adam_train(t->sites, t->adam, t->grads, t->tau_b, t->geom, t->color, hp, t->state,
-                      t->n, t->w, t->h, s);
+    launch_adam_train(t->sites, t->adam, t->grads, t->tau_nbr, t->tau_raw, t->tau_active, t->tau_a,
+                      t->geom, t->color, hp, t->state, t->cfg.iterations, t->n, t->w, t->h, s);
     if (prune) {
         float delta_norm = 1.0f / std::max(1.0f, t->mask_sum);
         launch_prune_pairs_fixed(t->sites, t->grads, t->removal_mul, t->pairs, t->n, delta_norm,
@@ -318,11 +322,14 @@ static sad_status_t run_densify(sad_trainer* t, const IterPlan& p, cudaStream_t 
 }
 
 static sad_status_t capture_variant(sad_trainer* t, bool upd, bool prune, int field,
-                                    cudaGraphExec_t* out) {
+                                    cudaGraphExec_t* out, uint64_t* kernels) {
     cudaGraph_t graph = nullptr;
     SAD_TRY(check_cuda(cudaStreamBeginCapture(t->st, cudaStreamCaptureModeThreadLocal),
                        "trainer graph capture"));
+    const uint64_t before = sad_launch_count();
     iteration_body(t, upd, prune, field, upd ? t->passes : 0, t->st);
+    *kernels = sad_launch_count() - before;
+    unnote_launches(*kernels);  // captured, not run; each replay counts them
     cudaError_t e = cudaStreamEndCapture(t->st, &graph);
     if (e != cudaSuccess) return check_cuda(e, "trainer graph capture end");
     e = cudaGraphInstantiate(out, graph, 0);
@@ -413,6 +420,9 @@ extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int wi
     ALLOC(t->grads, static_cast<size_t>(cap) * 12);
     ALLOC(t->tau_a, cap);
     ALLOC(t->tau_b, cap);
+    ALLOC(t->tau_nbr, static_cast<size_t>(cap) * 8);
+    ALLOC(t->tau_raw, cap);
+    ALLOC(t->tau_active, cap);
     ALLOC(t->pairs, static_cast<size_t>(cap) * 2);
     ALLOC(t->idx, SAD_MAX_SPLIT_INDICES);
     for (int b = 0; b < 3; ++b) {
@@ -425,7 +435,7 @@ extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int wi
     ALLOC(t->stats, static_cast<size_t>(cap) * 8);
     ALLOC(t->stats_fix, static_cast<size_t>(cap) * 8);
     ALLOC(t->render, np * 3);
-    ALLOC(t->metric, 4);
+    ALLOC(t->metric, 1);
     ALLOC(t->count, 4);
     ALLOC(t->state, 1);
     ALLOC(t->prune_k, std::max(1, cfg->iterations));
@@ -614,10 +624,10 @@ extern "C" sad_status_t sad_trainer_run(sad_trainer_t* t, int end) {
             t->cur = iteration_body(t, p.upd, p.prune, t->cur, p.upd ? t->passes : 0, t->st);
         } else {
             cudaGraphExec_t& g = t->graphs[p.upd][p.prune][t->cur];
-            if (!g) SAD_TRY(capture_variant(t, p.upd, p.prune, t->cur, &g));
+            uint64_t& nk = t->graph_kernels[p.upd][p.prune][t->cur];
+            if (!g) SAD_TRY(capture_variant(t, p.upd, p.prune, t->cur, &g, &nk));
             SAD_TRY(check_cuda(cudaGraphLaunch(g, t->st), "trainer graph launch"));
-            note_launches(p.upd ? (1 + t->passes + 7 + (p.prune ? 9 : 0))
-                                : (7 + (p.prune ? 9 : 0)));
+            note_launches(nk);
             if (p.upd) t->cur = refresh_target(t, t->cur);
         }
         SAD_TRY(check_launch("sad_trainer_run"));
@@ -648,12 +658,14 @@ extern "C" sad_status_t sad_trainer_render(sad_trainer_t* t, float* rgb_out, flo
                                            cudaMemcpyDeviceToDevice, t->st),
                            "trainer render copy"));
     if (psnr_out) {
-        float sum = 0.0f;
-        SAD_TRY(check_cuda(cudaMemsetAsync(t->metric, 0, 4, t->st), "trainer metric clear"));
-        launch_mse(t->render, t->target, t->have_mask ? t->mask : nullptr, t->metric, t->w, t->h, t->st);
-        SAD_TRY(check_cuda(cudaMemcpyAsync(&sum, t->metric, 4, cudaMemcpyDeviceToHost, t->st),
+        long long fsum = 0;
+        SAD_TRY(check_cuda(cudaMemsetAsync(t->metric, 0, sizeof(long long), t->st), "trainer metric clear"));
+        launch_mse_fixed(t->render, t->target, t->have_mask ? t->mask : nullptr, t->metric, t->w, t->h,
+                         t->st);
+        SAD_TRY(check_cuda(cudaMemcpyAsync(&fsum, t->metric, sizeof(long long), cudaMemcpyDeviceToHost, t->st),
                            "trainer metric copy"));
         SAD_TRY(check_cuda(cudaStreamSynchronize(t->st), "trainer render sync"));
+        float sum = static_cast<float>(static_cast<double>(fsum) * (1.0 / (1 << kFixFracBits)));
         float mse = sum / (std::max(1.0f, t->mask_sum) * 3.0f);
         *psnr_out = mse > 0.0f ? 20.0f * log10f(1.0f / sqrtf(mse)) : 100.0f;
     }
