@@ -2,7 +2,7 @@
 the identical 8-bit image (equal-PSNR speed comparison).  Prints one JSON line.
 
     oracle/ref/stage.sh /path/to/reference && oracle/ref/build.sh
-    python oracle/ref/time_reference.py [--repeats 2] [--size 1024]
+    python oracle/ref/time_reference.py [--repeats 2] [--size 1024] [--seeds 4]
 
 The reference binary (oracle/_ref/sad_cuda, built from the staged copy of its sources)
 reads training_config.json from its working directory (baseline/_ref/sad holds the staged
@@ -20,6 +20,8 @@ import subprocess
 import sys
 import tempfile
 import time
+
+import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -81,17 +83,28 @@ def main():
     ap.add_argument("--repeats", type=int, default=2)
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--log-freq", type=int, default=1000)
+    ap.add_argument("--seeds", type=int, default=1, help="images: synthetic seeds 0..N-1")
     args = ap.parse_args()
     from sad_gb300 import imageio
     from sad_gb300.synthetic import quantize_u8, synthetic_image
-    img = quantize_u8(synthetic_image(args.size, args.size, seed=0))
-    png = os.path.join(tempfile.mkdtemp(), f"synthetic_{args.size}.png")
-    imageio.save_image(png, img)
-    ref = run_reference(png, args.repeats, args.log_freq)
-    ours = run_ours(img, args.repeats)
+    per_seed = []
+    for seed in range(args.seeds):
+        img = quantize_u8(synthetic_image(args.size, args.size, seed=seed))
+        png = os.path.join(tempfile.mkdtemp(), f"synthetic_{args.size}_s{seed}.png")
+        imageio.save_image(png, img)
+        ref = run_reference(png, args.repeats, args.log_freq)
+        ours = run_ours(img, args.repeats)
+        per_seed.append({"seed": seed, "reference_cuda_cli": ref, "ours": ours,
+                         "speedup_it_per_s": round(ours["it_per_s"] / ref["it_per_s"], 2)
+                         if ref.get("it_per_s") else None})
+    mean = lambda xs: round(float(np.mean(xs)), 3)
     out = {"workload": f"{args.size}x{args.size} synthetic (8-bit), training_config.json defaults",
-           "reference_cuda_cli": ref, "ours": ours,
-           "speedup_it_per_s": round(ours["it_per_s"] / ref["it_per_s"], 2) if ref.get("it_per_s") else None}
+           "seeds": args.seeds, "per_seed": per_seed,
+           "reference_it_per_s_mean": mean([p["reference_cuda_cli"]["it_per_s"] for p in per_seed]),
+           "ours_it_per_s_mean": mean([p["ours"]["it_per_s"] for p in per_seed]),
+           "reference_psnr_mean": mean([p["reference_cuda_cli"]["psnr_db"] for p in per_seed]),
+           "ours_psnr_mean": mean([p["ours"]["psnr_db"] for p in per_seed])}
+    out["speedup_it_per_s"] = round(out["ours_it_per_s_mean"] / out["reference_it_per_s_mean"], 2)
     print(json.dumps(out))
 
 
