@@ -107,6 +107,7 @@ struct PackedGeomSites {
 template <int L>
 __device__ __forceinline__ void sorted_insert(uint32_t (&bi)[L], float (&bd)[L], uint32_t id,
                                               float d) {
+    if (!(d < bd[L - 1])) return;  // not better than the last entry: no slot takes it
 #pragma unroll
     for (int j = L - 1; j > 0; --j) {
         bool before_prev = d < bd[j - 1];
