@@ -146,6 +146,10 @@ struct TileTable<NV, SLOTS, AccFloat> : KeyTable<SLOTS> {
             for (int k = 0; k < NV; ++k) vals[k][i] = 0.0f;
         }
     }
+    __device__ __forceinline__ void zero(int d) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) vals[k][d] = 0.0f;
+    }
     __device__ __forceinline__ void add(int d, const float (&v)[NV]) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) atomicAdd(&vals[k][d], v[k]);
@@ -170,6 +174,13 @@ struct TileTable<NV, SLOTS, AccSplit> : KeyTable<SLOTS> {
                 hi[k][i] = 0;
                 lo[k][i] = 0;
             }
+        }
+    }
+    __device__ __forceinline__ void zero(int d) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            hi[k][d] = 0;
+            lo[k][d] = 0;
         }
     }
     __device__ __forceinline__ void add(int d, const float (&v)[NV]) {

@@ -24,7 +24,7 @@
 
 namespace sad {
 
-constexpr int kGradSlots = 512;
+constexpr int kGradSlots = kTileKeys;
 constexpr float kRemovalSentinel = 1.0e6f;  // removal delta of a pixel the site dominates
 
 __device__ __forceinline__ float luma(const float* __restrict__ p) {
@@ -115,13 +115,25 @@ struct GradLayout {
     using Table = TileTable<NV, kGradSlots, Mode>;
 };
 
-template <class Src, bool kFix, bool kRemoval, bool kSSIM>
+template <class Src, bool kFix, bool kRemoval, bool kSSIM, bool kPre>
 __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm, Src src) {
     using L = GradLayout<kFix, kRemoval>;
     constexpr int NV = L::NV;
     auto& table = shared_table<typename L::Table>();
     const int tid = threadIdx.x;
-    table.init(tid, 256);
+    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    if constexpr (kPre) {
+        // the tile's keys were registered when its candidate field was built
+        const int used = prm.tile_count[tile];
+        const uint32_t* keys = prm.tile_keys + static_cast<size_t>(tile) * kTileKeys;
+        for (int d = tid; d < used; d += 256) {
+            table.dkey[d] = keys[d];
+            table.zero(d);
+        }
+        if (tid == 0) table.count = used;
+    } else {
+        table.init(tid, 256);
+    }
     __syncthreads();
 
     const int lane = tid & 31, warp = tid >> 5;
@@ -235,11 +247,22 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
         }
     }
 
-    // 1. one CAS per (warp, site): register every candidate of the warp in the table
+    // 1. table index of every candidate: precomputed, or one CAS per (warp, site)
     int slots[kCand];
+    if constexpr (kPre) {
+        uint4 m = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
+        if (x < w && y < h) m = __ldg(prm.slot_map + static_cast<size_t>(y) * w + x);
+        const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
 #pragma unroll
-    for (int i = 0; i < kCand; ++i)
-        slots[i] = register_key(table, (valid >> i & 1u) ? ids[i] : kEmpty);
+        for (int i = 0; i < kCand; ++i) {
+            uint32_t sidx = (mw[i >> 1] >> (16 * (i & 1))) & 0xFFFFu;
+            slots[i] = ((valid >> i & 1u) && sidx != 0xFFFFu) ? static_cast<int>(sidx) : -1;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kCand; ++i)
+            slots[i] = register_key(table, (valid >> i & 1u) ? ids[i] : kEmpty);
+    }
 
     // 2. accumulate in a lane-rotated candidate order; the loop is kept rolled (the arrays
     // shift down one entry per step) so the kernel body stays small in the instruction cache
@@ -285,11 +308,78 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
     for (int d = tid; d < used; d += 256) flush_slot<kFix, NV>(prm, table, d);
 }
 
+// Tile registration of a candidate field: the table index of each (pixel, candidate)
+// and each tile's key list, with the gradient kernel's tiling (16x16 tiles, 8x4 warp
+// patches) and its registration (one CAS per warp and site).  Every candidate id below
+// n is registered; inactive sites simply receive no value.
+__global__ void __launch_bounds__(256) register_tiles_kernel(const uint4* __restrict__ c0,
+                                                             const uint4* __restrict__ c1, uint32_t n,
+                                                             int w, int h, int cw, int ch, TileMap map) {
+    __shared__ KeyTable<kTileKeys> table;
+    const int tid = threadIdx.x;
+    table.init_keys(tid, 256);
+    __syncthreads();
+    const int lane = tid & 31, warp = tid >> 5;
+    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    const int y = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+    const bool inside = x < w && y < h;
+    uint32_t ids[kCand];
+    if (inside) {
+        int ci = cand_index_for_pixel(x, y, w, h, cw, ch);
+        uint4 a = __ldg(c0 + ci), b = __ldg(c1 + ci);
+        ids[0] = a.x; ids[1] = a.y; ids[2] = a.z; ids[3] = a.w;
+        ids[4] = b.x; ids[5] = b.y; ids[6] = b.z; ids[7] = b.w;
+    } else {
+#pragma unroll
+        for (int i = 0; i < kCand; ++i) ids[i] = kEmpty;
+    }
+    uint32_t packed[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int i = 0; i < kCand; ++i) {
+        int slot = register_key(table, ids[i] < n ? ids[i] : kEmpty);
+        uint32_t sidx = slot < 0 ? 0xFFFFu : static_cast<uint32_t>(slot);
+        packed[i >> 1] |= sidx << (16 * (i & 1));
+    }
+    if (inside)
+        map.slot_map[static_cast<size_t>(y) * w + x] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    __syncthreads();
+    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int used = table.size();
+    for (int d = tid; d < used; d += 256) map.tile_keys[static_cast<size_t>(tile) * kTileKeys + d] = table.key_at(d);
+    if (tid == 0) map.tile_count[tile] = used;
+}
+
+size_t tile_map_words(int w, int h) {
+    size_t tiles = static_cast<size_t>((w + 15) / 16) * ((h + 15) / 16);
+    return static_cast<size_t>(w) * h * 4 + tiles * kTileKeys + tiles;
+}
+
+TileMap tile_map_at(uint32_t* base, int w, int h) {
+    size_t tiles = static_cast<size_t>((w + 15) / 16) * ((h + 15) / 16);
+    TileMap m;
+    m.slot_map = reinterpret_cast<uint4*>(base);
+    m.tile_keys = base + static_cast<size_t>(w) * h * 4;
+    m.tile_count = reinterpret_cast<int*>(m.tile_keys + tiles * kTileKeys);
+    return m;
+}
+
+void launch_register_tiles(const uint32_t* c0, const uint32_t* c1, uint32_t n, int w, int h,
+                           int cw, int ch, const TileMap& map, cudaStream_t st) {
+    dim3 grid((w + 15) / 16, (h + 15) / 16);
+    register_tiles_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const uint4*>(c0),
+                                                  reinterpret_cast<const uint4*>(c1), n, w, h, cw, ch,
+                                                  map);
+    note_launches(1);
+}
+
 template <class Src, bool kFix, bool kRemoval, bool kSSIM>
 static void launch_fused(const GradParams& p, Src src, cudaStream_t st) {
     dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
     size_t smem = sizeof(typename GradLayout<kFix, kRemoval>::Table);
-    fused_gradients_kernel<Src, kFix, kRemoval, kSSIM><<<grid, 256, smem, st>>>(p, src);
+    if (p.slot_map)
+        fused_gradients_kernel<Src, kFix, kRemoval, kSSIM, true><<<grid, 256, smem, st>>>(p, src);
+    else
+        fused_gradients_kernel<Src, kFix, kRemoval, kSSIM, false><<<grid, 256, smem, st>>>(p, src);
 }
 
 cudaError_t prepare_gradient_kernels();
@@ -324,9 +414,11 @@ static void dispatch_gradients(const GradParams& p, Src src, cudaStream_t st) {
 template <class Src, bool kFix, bool kRemoval>
 static cudaError_t allow_variant() {
     size_t smem = sizeof(typename GradLayout<kFix, kRemoval>::Table);
-    cudaError_t e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false>, smem);
-    if (e != cudaSuccess) return e;
-    return allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true>, smem);
+    cudaError_t e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false, false>, smem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true, false>, smem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false, true>, smem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true, true>, smem);
+    return e;
 }
 
 cudaError_t prepare_gradient_kernels() {

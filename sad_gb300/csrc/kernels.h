@@ -85,7 +85,24 @@ struct GradParams {
     long long* fix12;
     float removal_fix_mul;  // fixed-point path: removal delta pre-scale (power of two <= 1)
     int compute_removal;
+    // trainer: the candidate field's tile registration, computed once per field refresh
+    // (nullptr: register keys inside the gradient kernel)
+    const uint4* slot_map;     // [H*W] 8 x u16 tile-table index per candidate, 0xFFFF none
+    const uint32_t* tile_keys;  // [tiles][kTileKeys] keys by table index
+    const int* tile_count;      // [tiles] keys in use
 };
+// Keys a 16x16 tile's accumulation table holds; the registration is precomputable because
+// it depends only on the candidate field (which changes once per VPT refresh).
+constexpr int kTileKeys = 512;
+struct TileMap {
+    uint4* slot_map;
+    uint32_t* tile_keys;
+    int* tile_count;
+};
+size_t tile_map_words(int w, int h);  // u32 words of one TileMap (slot map + keys + counts)
+TileMap tile_map_at(uint32_t* base, int w, int h);
+void launch_register_tiles(const uint32_t* c0, const uint32_t* c1, uint32_t n, int w, int h,
+                           int cw, int ch, const TileMap& map, cudaStream_t st);
 void launch_gradients_raw(const GradParams& p, const Site* sites, cudaStream_t st);
 // Opts the >48 KB shared-memory variants in; call once per device before any capture.
 cudaError_t prepare_gradient_kernels();

@@ -78,6 +78,8 @@ struct sad_trainer {
     uint32_t* idx = nullptr;
     uint32_t* cand0[3] = {nullptr, nullptr, nullptr};
     uint32_t* cand1[3] = {nullptr, nullptr, nullptr};
+    uint32_t* tmap_mem[3] = {nullptr, nullptr, nullptr};
+    sad::TileMap tmap[3] = {};  // tile registration of each candidate field
     uint32_t* horder = nullptr;
     uint32_t* hpos = nullptr;
     uint32_t* hpairs = nullptr;
@@ -223,6 +225,8 @@ static int launch_refresh(sad_trainer* t, int src, cudaStream_t s) {
         launch_vpt_geom(p, t->vgeom, s);
         in = out;
     }
+    if (t->passes > 0)
+        launch_register_tiles(t->cand0[in], t->cand1[in], t->n, t->w, t->h, t->cw, t->ch, t->tmap[in], s);
     return in;
 }
 
@@ -248,6 +252,9 @@ static void launch_gradients_step(sad_trainer* t, int field, bool prune, cudaStr
     g.cand_width = t->cw;
     g.cand_height = t->ch;
     g.fix12 = t->grads;
+    g.slot_map = t->tmap[field].slot_map;
+    g.tile_keys = t->tmap[field].tile_keys;
+    g.tile_count = t->tmap[field].tile_count;
     g.removal_fix_mul = t->removal_mul;
     g.compute_removal = prune ? 1 : 0;
     launch_gradients_prepared(g, t->geom, t->color, s);
@@ -428,6 +435,8 @@ extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int wi
     for (int b = 0; b < 3; ++b) {
         ALLOC(t->cand0[b], nc);
         ALLOC(t->cand1[b], nc);
+        ALLOC(t->tmap_mem[b], tile_map_words(width, height));
+        if (s == SAD_OK) t->tmap[b] = tile_map_at(t->tmap_mem[b], width, height);
     }
     ALLOC(t->horder, cap);
     ALLOC(t->hpos, cap);
@@ -579,6 +588,7 @@ extern "C" sad_status_t sad_trainer_init(sad_trainer_t* t, const float* sites_ho
     t->hilbert_ready = false;
     launch_init_candidates(t->cand0[0], t->cand1[0], n0, 0u, 0, t->cw, t->ch, s);
     launch_jfa_seed(t->cand0[0], t->sites, n0, t->cw, t->ch, t->ds, s);
+    launch_register_tiles(t->cand0[0], t->cand1[0], n0, t->w, t->h, t->cw, t->ch, t->tmap[0], s);
     make_plan(t);
     std::vector<uint32_t> pk(std::max(1, t->cfg.iterations), 0u);
     for (size_t i = 0; i < t->plan.size(); ++i) pk[i] = t->plan[i].prune_k;
