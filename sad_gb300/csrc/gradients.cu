@@ -113,22 +113,53 @@ struct GradLayout {
     static constexpr int NV = kRemoval ? (kFix ? 12 : 11) : 10;
     using Mode = typename std::conditional<kFix, AccSplit, AccFloat>::type;
     using Table = TileTable<NV, kGradSlots, Mode>;
+    // with a precomputed registration the tile's sites are also staged in shared memory
+    struct Staged {
+        Table table;
+        float4 g0[kGradSlots];   // px, py, tau, radius
+        float4 g1[kGradSlots];   // dx, dy, l1, l2
+        float4 col[kGradSlots];  // r, g, b, -
+    };
 };
+
+// Site data of candidate `slot` of the tile: staged in shared memory, or read directly
+// when the candidate is not in the tile's table.
+template <class Staged, class Src>
+__device__ __forceinline__ void staged_site(const Staged& sm, const Src& src, uint32_t id, int slot,
+                                            SiteGeom& g, float3& c) {
+    if (slot >= 0) {
+        float4 a = sm.g0[slot], b = sm.g1[slot], q = sm.col[slot];
+        g.px = a.x; g.py = a.y; g.tau = a.z; g.radius = a.w;
+        g.dx = b.x; g.dy = b.y; g.l1 = b.z; g.l2 = b.w;
+        c = make_float3(q.x, q.y, q.z);
+    } else {
+        src.load(id, g, c);
+    }
+}
 
 template <class Src, bool kFix, bool kRemoval, bool kSSIM, bool kPre>
 __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm, Src src) {
     using L = GradLayout<kFix, kRemoval>;
     constexpr int NV = L::NV;
-    auto& table = shared_table<typename L::Table>();
+    auto& sm = shared_table<typename L::Staged>();
+    auto& table = sm.table;
     const int tid = threadIdx.x;
     const int tile = blockIdx.y * gridDim.x + blockIdx.x;
     if constexpr (kPre) {
-        // the tile's keys were registered when its candidate field was built
+        // the tile's keys were registered when its candidate field was built: clear their
+        // values and stage their sites
         const int used = prm.tile_count[tile];
         const uint32_t* keys = prm.tile_keys + static_cast<size_t>(tile) * kTileKeys;
         for (int d = tid; d < used; d += 256) {
-            table.dkey[d] = keys[d];
+            const uint32_t key = keys[d];
+            table.dkey[d] = key;
             table.zero(d);
+            SiteGeom g;
+            float3 c;
+            src.load(key, g, c);
+            sm.g0[d] = make_float4(g.px, g.py, g.tau, g.radius);
+            sm.g1[d] = make_float4(g.dx, g.dy, g.l1, g.l2);
+            sm.col[d] = make_float4(c.x, c.y, c.z, 0.0f);
         }
         if (tid == 0) table.count = used;
     } else {
@@ -157,6 +188,20 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
         rem[i] = 0.0f;
     }
 
+    // table index of each candidate when the registration is precomputed: 8 x u16 packed
+    // in 4 words, 0xFFFF = not in the table
+    uint32_t pm[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    if constexpr (kPre) {
+        if (x < w && y < h) {
+            uint4 m = __ldg(prm.slot_map + static_cast<size_t>(y) * w + x);
+            pm[0] = m.x; pm[1] = m.y; pm[2] = m.z; pm[3] = m.w;
+        }
+    }
+    auto pre = [&pm](int i) {
+        uint32_t sidx = (pm[i >> 1] >> (16 * (i & 1))) & 0xFFFFu;
+        return sidx == 0xFFFFu ? -1 : static_cast<int>(sidx);
+    };
+
     bool live = x < w && y < h;
     int pix = live ? y * w + x : 0;
     if (live && prm.mask) live = __ldg(prm.mask + pix) > 0.0f;
@@ -175,7 +220,10 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
             cols[i] = make_float3(0.f, 0.f, 0.f);
             if (ids[i] >= n) continue;
             SiteGeom g;
-            src.load(ids[i], g, cols[i]);
+            if constexpr (kPre)
+                staged_site(sm, src, ids[i], pre(i), g, cols[i]);
+            else
+                src.load(ids[i], g, cols[i]);
             if (g.px < 0.0f) continue;
             valid |= 1u << i;
             if (g.px >= 0.0f) blend |= 1u << i;
@@ -250,14 +298,8 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
     // 1. table index of every candidate: precomputed, or one CAS per (warp, site)
     int slots[kCand];
     if constexpr (kPre) {
-        uint4 m = make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
-        if (x < w && y < h) m = __ldg(prm.slot_map + static_cast<size_t>(y) * w + x);
-        const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
 #pragma unroll
-        for (int i = 0; i < kCand; ++i) {
-            uint32_t sidx = (mw[i >> 1] >> (16 * (i & 1))) & 0xFFFFu;
-            slots[i] = ((valid >> i & 1u) && sidx != 0xFFFFu) ? static_cast<int>(sidx) : -1;
-        }
+        for (int i = 0; i < kCand; ++i) slots[i] = (valid >> i & 1u) ? pre(i) : -1;
     } else {
 #pragma unroll
         for (int i = 0; i < kCand; ++i)
@@ -277,7 +319,10 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
         if (vr & 1u) {
             SiteGeom g;
             float3 col;
-            src.load(ids[0], g, col);
+            if constexpr (kPre)
+                staged_site(sm, src, ids[0], slots[0], g, col);
+            else
+                src.load(ids[0], g, col);
             float o[10];
             candidate_grads(g, col, ux, uy, inv_s2, inv_scale, wts[0], dLdp, pred, true, o);
             float v[NV];
@@ -375,11 +420,12 @@ void launch_register_tiles(const uint32_t* c0, const uint32_t* c1, uint32_t n, i
 template <class Src, bool kFix, bool kRemoval, bool kSSIM>
 static void launch_fused(const GradParams& p, Src src, cudaStream_t st) {
     dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
-    size_t smem = sizeof(typename GradLayout<kFix, kRemoval>::Table);
     if (p.slot_map)
-        fused_gradients_kernel<Src, kFix, kRemoval, kSSIM, true><<<grid, 256, smem, st>>>(p, src);
+        fused_gradients_kernel<Src, kFix, kRemoval, kSSIM, true>
+            <<<grid, 256, sizeof(typename GradLayout<kFix, kRemoval>::Staged), st>>>(p, src);
     else
-        fused_gradients_kernel<Src, kFix, kRemoval, kSSIM, false><<<grid, 256, smem, st>>>(p, src);
+        fused_gradients_kernel<Src, kFix, kRemoval, kSSIM, false>
+            <<<grid, 256, sizeof(typename GradLayout<kFix, kRemoval>::Table), st>>>(p, src);
 }
 
 cudaError_t prepare_gradient_kernels();
@@ -414,10 +460,11 @@ static void dispatch_gradients(const GradParams& p, Src src, cudaStream_t st) {
 template <class Src, bool kFix, bool kRemoval>
 static cudaError_t allow_variant() {
     size_t smem = sizeof(typename GradLayout<kFix, kRemoval>::Table);
+    size_t staged = sizeof(typename GradLayout<kFix, kRemoval>::Staged);
     cudaError_t e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false, false>, smem);
     if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true, false>, smem);
-    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false, true>, smem);
-    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true, true>, smem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false, true>, staged);
+    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true, true>, staged);
     return e;
 }
 
