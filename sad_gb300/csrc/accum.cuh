@@ -132,20 +132,14 @@ struct KeyTable {
     __device__ __forceinline__ uint32_t key_at(int d) const { return dkey[d]; }
 };
 
-template <int NV, int SLOTS, class Mode>
-struct TileTable;
+// Values of a tile table: NV values per dense index.
+template <int NV, int N, class Mode>
+struct TileValues;
 
-template <int NV, int SLOTS>
-struct TileTable<NV, SLOTS, AccFloat> : KeyTable<SLOTS> {
-    float vals[NV][SLOTS];
+template <int NV, int N>
+struct TileValues<NV, N, AccFloat> {
+    float vals[NV][N];
 
-    __device__ __forceinline__ void init(int tid, int nthreads) {
-        this->init_keys(tid, nthreads);
-        for (int i = tid; i < SLOTS; i += nthreads) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) vals[k][i] = 0.0f;
-        }
-    }
     __device__ __forceinline__ void zero(int d) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) vals[k][d] = 0.0f;
@@ -161,21 +155,11 @@ struct TileTable<NV, SLOTS, AccFloat> : KeyTable<SLOTS> {
 // Fixed-point words: x = to_fix(v) = hi * 2^20 + lo with |lo| <= 2^19, so the lo sum of
 // up to 2^11 terms fits an int32 and hi (zero for |v| < 2^-5, then skipped) wraps modulo
 // 2^32, which the recombination absorbs while the tile's total stays below 2^27.
-template <int NV, int SLOTS>
-struct TileTable<NV, SLOTS, AccSplit> : KeyTable<SLOTS> {
-    int hi[NV][SLOTS];
-    int lo[NV][SLOTS];
+template <int NV, int N>
+struct TileValues<NV, N, AccSplit> {
+    int hi[NV][N];
+    int lo[NV][N];
 
-    __device__ __forceinline__ void init(int tid, int nthreads) {
-        this->init_keys(tid, nthreads);
-        for (int i = tid; i < SLOTS; i += nthreads) {
-#pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                hi[k][i] = 0;
-                lo[k][i] = 0;
-            }
-        }
-    }
     __device__ __forceinline__ void zero(int d) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
@@ -194,6 +178,15 @@ struct TileTable<NV, SLOTS, AccSplit> : KeyTable<SLOTS> {
     }
     __device__ __forceinline__ long long fixed(int k, int d) const {
         return static_cast<long long>(hi[k][d]) * (1ll << kSplitLoBits) + static_cast<long long>(lo[k][d]);
+    }
+};
+
+// Keys and values of one tile (keys registered in the kernel).
+template <int NV, int SLOTS, class Mode>
+struct TileTable : KeyTable<SLOTS>, TileValues<NV, SLOTS, Mode> {
+    __device__ __forceinline__ void init(int tid, int nthreads) {
+        this->init_keys(tid, nthreads);
+        for (int i = tid; i < SLOTS; i += nthreads) this->zero(i);
     }
 };
 

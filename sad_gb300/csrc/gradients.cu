@@ -24,7 +24,7 @@
 
 namespace sad {
 
-constexpr int kGradSlots = kTileKeys;
+constexpr int kGradSlots = 512;  // hash slots (and values) of the in-kernel registration table
 constexpr float kRemovalSentinel = 1.0e6f;  // removal delta of a pixel the site dominates
 
 __device__ __forceinline__ float luma(const float* __restrict__ p) {
@@ -105,6 +105,18 @@ __device__ __forceinline__ void flush_slot(const GradParams& p, const Table& tab
     }
 }
 
+// Flush of one table entry of the precomputed-registration kernel (fixed point).
+template <int NV, class Values>
+__device__ __forceinline__ void flush_values(const GradParams& p, const Values& vals, uint32_t key,
+                                             int d) {
+    long long* o = p.fix12 + static_cast<size_t>(key) * 12;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        long long v = vals.fixed(k, d);
+        if (v != 0) fix_add_global(o + k, v);
+    }
+}
+
 // Values per table slot: 10 gradients, + removal delta (float path), + removal delta and
 // count of "keep < 1e-4" pixels (fixed-point path; each such pixel adds the reference's
 // 1e6 sentinel, kept as an exact integer count so the fixed-point sum cannot overflow).
@@ -113,65 +125,145 @@ struct GradLayout {
     static constexpr int NV = kRemoval ? (kFix ? 12 : 11) : 10;
     using Mode = typename std::conditional<kFix, AccSplit, AccFloat>::type;
     using Table = TileTable<NV, kGradSlots, Mode>;
-    // with a precomputed registration the tile's sites are also staged in shared memory
-    struct Staged {
-        Table table;
-        float4 g0[kGradSlots];   // px, py, tau, radius
-        float4 g1[kGradSlots];   // dx, dy, l1, l2
-        float4 col[kGradSlots];  // r, g, b, -
+    // precomputed registration (trainer): the tile's values, keys and staged sites, and
+    // each thread's candidate weights (and removal deltas) for the accumulation loop
+    struct Pre {
+        TileValues<NV, kTileKeys, Mode> vals;
+        uint32_t dkey[kTileKeys];
+        float4 g0[kTileKeys];  // px, py, tau, radius
+        float4 g1[kTileKeys];  // dx, dy, l1, l2
+        float4 col[kTileKeys];  // r, g, b, -
+        float wts[kCand][256];
+        float rem[kRemoval ? kCand : 1][256];
     };
 };
 
-// Site data of candidate `slot` of the tile: staged in shared memory, or read directly
-// when the candidate is not in the tile's table.
-template <class Staged, class Src>
-__device__ __forceinline__ void staged_site(const Staged& sm, const Src& src, uint32_t id, int slot,
-                                            SiteGeom& g, float3& c) {
-    if (slot >= 0) {
-        float4 a = sm.g0[slot], b = sm.g1[slot], q = sm.col[slot];
-        g.px = a.x; g.py = a.y; g.tau = a.z; g.radius = a.w;
-        g.dx = b.x; g.dy = b.y; g.l1 = b.z; g.l2 = b.w;
-        c = make_float3(q.x, q.y, q.z);
-    } else {
-        src.load(id, g, c);
+// Forward of one pixel: softmax over the 8 candidates, pred, dL/dpred (+ SSIM term) and,
+// with kRemoval, the removal delta on the first slot of each distinct valid site.
+// site(i, g, col) supplies candidate i's data.  Semantics of
+// backends/cuda/src/gradients.cu:103-300.
+template <bool kRemoval, bool kSSIM, class SiteFn>
+__device__ __forceinline__ void pixel_forward(const GradParams& prm, int x, int y, float ux,
+                                              float uy, float inv_s2, float inv_scale,
+                                              const uint32_t (&ids)[kCand], float3 tgt,
+                                              SiteFn site, float (&wts)[kCand],
+                                              float (&rem)[kCand], uint32_t& valid,
+                                              float3& pred, float3& dLdp) {
+    const uint32_t n = prm.site_count;
+    uint32_t blend = 0;
+    float logits[kCand];
+    float3 cols[kCand];
+    float mx = -INFINITY;
+#pragma unroll
+    for (int i = 0; i < kCand; ++i) {
+        logits[i] = -INFINITY;
+        cols[i] = make_float3(0.f, 0.f, 0.f);
+        if (ids[i] >= n) continue;
+        SiteGeom g;
+        site(i, g, cols[i]);
+        if (g.px < 0.0f) continue;
+        valid |= 1u << i;
+        if (g.px >= 0.0f) blend |= 1u << i;
+        float tau = g.tau;
+        float d = dmix2(g, ux, uy, inv_s2, inv_scale);
+        logits[i] = -tau * d;
+        mx = fmaxf(mx, logits[i]);
+    }
+    if (isinf(mx) && mx < 0.0f) {
+        valid = 0;
+        return;
+    }
+    float sum = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kCand; ++i) {
+        wts[i] = expf(logits[i] - mx);
+        sum += wts[i];
+    }
+    float inv_sum = 1.0f / fmaxf(sum, 1e-8f);
+#pragma unroll
+    for (int i = 0; i < kCand; ++i) {
+        wts[i] *= inv_sum;
+        if (blend >> i & 1u) {
+            pred.x += wts[i] * cols[i].x;
+            pred.y += wts[i] * cols[i].y;
+            pred.z += wts[i] * cols[i].z;
+        }
+    }
+    dLdp = make_float3(2.0f * (pred.x - tgt.x), 2.0f * (pred.y - tgt.y), 2.0f * (pred.z - tgt.z));
+    if constexpr (kSSIM) {
+        float ds = ssim_dloss(prm.rendered, prm.target, x, y, prm.width, prm.height);
+        float k = -prm.ssim_weight * ds;
+        dLdp.x += k * 0.299f;
+        dLdp.y += k * 0.587f;
+        dLdp.z += k * 0.114f;
+    }
+    if constexpr (kRemoval) {
+#pragma unroll
+        for (int i = 0; i < kCand; ++i) {
+            if (!(valid >> i & 1u)) continue;
+            bool first = true;
+#pragma unroll
+            for (int j = 0; j < i; ++j) first &= !((valid >> j & 1u) && ids[j] == ids[i]);
+            if (!first) continue;
+            float wt = 0.0f;
+#pragma unroll
+            for (int j = i; j < kCand; ++j)
+                if ((valid >> j & 1u) && ids[j] == ids[i]) wt += wts[j];
+            if (!(wt > 0.0f)) continue;
+            float keep = 1.0f - wt;
+            float delta;
+            if (keep < 1e-4f) {
+                delta = kRemovalSentinel;
+            } else {
+                float3 c = cols[i];
+                float3 pk = make_float3((pred.x - wt * c.x) / keep, (pred.y - wt * c.y) / keep,
+                                        (pred.z - wt * c.z) / keep);
+                float3 df = make_float3(pred.x - tgt.x, pred.y - tgt.y, pred.z - tgt.z);
+                float3 dk = make_float3(pk.x - tgt.x, pk.y - tgt.y, pk.z - tgt.z);
+                delta = (dk.x * dk.x + dk.y * dk.y + dk.z * dk.z) -
+                        (df.x * df.x + df.y * df.y + df.z * df.z);
+            }
+            rem[i] = delta;
+        }
     }
 }
 
-template <class Src, bool kFix, bool kRemoval, bool kSSIM, bool kPre>
+// The 10 (+ removal) values one candidate adds; the removal slots follow the table mode.
+template <bool kFix, int NV>
+__device__ __forceinline__ void candidate_values(const SiteGeom& g, float3 col, float ux, float uy,
+                                                 float inv_s2, float inv_scale, float w, float3 dLdp,
+                                                 float3 pred, float rem, float removal_fix_mul,
+                                                 float (&v)[NV]) {
+    float o[10];
+    candidate_grads(g, col, ux, uy, inv_s2, inv_scale, w, dLdp, pred, true, o);
+#pragma unroll
+    for (int k = 0; k < 10; ++k) v[k] = o[k];
+    if constexpr (NV > 10) {
+        if constexpr (kFix) {
+            bool sentinel = rem == kRemovalSentinel;
+            v[10] = sentinel ? 0.0f : rem * removal_fix_mul;
+            v[11] = sentinel ? kFixInvScale : 0.0f;  // adds exactly 1
+        } else {
+            v[10] = rem;
+        }
+    }
+}
+
+// One 16x16 tile per 256-thread block, each warp an 8x4 pixel patch, so the lanes of a
+// warp share most candidates.  Keys are registered here: one CAS per (warp, site).
+template <class Src, bool kFix, bool kRemoval, bool kSSIM>
 __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm, Src src) {
     using L = GradLayout<kFix, kRemoval>;
     constexpr int NV = L::NV;
-    auto& sm = shared_table<typename L::Staged>();
-    auto& table = sm.table;
+    auto& table = shared_table<typename L::Table>();
     const int tid = threadIdx.x;
-    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
-    if constexpr (kPre) {
-        // the tile's keys were registered when its candidate field was built: clear their
-        // values and stage their sites
-        const int used = prm.tile_count[tile];
-        const uint32_t* keys = prm.tile_keys + static_cast<size_t>(tile) * kTileKeys;
-        for (int d = tid; d < used; d += 256) {
-            const uint32_t key = keys[d];
-            table.dkey[d] = key;
-            table.zero(d);
-            SiteGeom g;
-            float3 c;
-            src.load(key, g, c);
-            sm.g0[d] = make_float4(g.px, g.py, g.tau, g.radius);
-            sm.g1[d] = make_float4(g.dx, g.dy, g.l1, g.l2);
-            sm.col[d] = make_float4(c.x, c.y, c.z, 0.0f);
-        }
-        if (tid == 0) table.count = used;
-    } else {
-        table.init(tid, 256);
-    }
+    table.init(tid, 256);
     __syncthreads();
 
     const int lane = tid & 31, warp = tid >> 5;
     const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
     const int y = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
     const int w = prm.width, h = prm.height;
-    const uint32_t n = prm.site_count;
     const float inv_s2 = prm.inv_scale_sq;
     const float inv_scale = sqrtf(inv_s2);
     const float ux = static_cast<float>(x), uy = static_cast<float>(y);
@@ -179,7 +271,7 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
     uint32_t ids[kCand];
     float wts[kCand];
     float rem[kCand];
-    uint32_t valid = 0, blend = 0;
+    uint32_t valid = 0;
     float3 pred = make_float3(0.f, 0.f, 0.f), dLdp = make_float3(0.f, 0.f, 0.f);
 #pragma unroll
     for (int i = 0; i < kCand; ++i) {
@@ -187,23 +279,8 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
         wts[i] = 0.0f;
         rem[i] = 0.0f;
     }
-
-    // table index of each candidate when the registration is precomputed: 8 x u16 packed
-    // in 4 words, 0xFFFF = not in the table
-    uint32_t pm[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
-    if constexpr (kPre) {
-        if (x < w && y < h) {
-            uint4 m = __ldg(prm.slot_map + static_cast<size_t>(y) * w + x);
-            pm[0] = m.x; pm[1] = m.y; pm[2] = m.z; pm[3] = m.w;
-        }
-    }
-    auto pre = [&pm](int i) {
-        uint32_t sidx = (pm[i >> 1] >> (16 * (i & 1))) & 0xFFFFu;
-        return sidx == 0xFFFFu ? -1 : static_cast<int>(sidx);
-    };
-
     bool live = x < w && y < h;
-    int pix = live ? y * w + x : 0;
+    const int pix = live ? y * w + x : 0;
     if (live && prm.mask) live = __ldg(prm.mask + pix) > 0.0f;
     if (live) {
         int ci = cand_index_for_pixel(x, y, w, h, prm.cand_width, prm.cand_height);
@@ -211,100 +288,18 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
         uint4 b = __ldg(reinterpret_cast<const uint4*>(prm.cand1) + ci);
         ids[0] = a.x; ids[1] = a.y; ids[2] = a.z; ids[3] = a.w;
         ids[4] = b.x; ids[5] = b.y; ids[6] = b.z; ids[7] = b.w;
-        float logits[kCand];
-        float3 cols[kCand];
-        float mx = -INFINITY;
-#pragma unroll
-        for (int i = 0; i < kCand; ++i) {
-            logits[i] = -INFINITY;
-            cols[i] = make_float3(0.f, 0.f, 0.f);
-            if (ids[i] >= n) continue;
-            SiteGeom g;
-            if constexpr (kPre)
-                staged_site(sm, src, ids[i], pre(i), g, cols[i]);
-            else
-                src.load(ids[i], g, cols[i]);
-            if (g.px < 0.0f) continue;
-            valid |= 1u << i;
-            if (g.px >= 0.0f) blend |= 1u << i;
-            float tau = g.tau;
-            float d = dmix2(g, ux, uy, inv_s2, inv_scale);
-            logits[i] = -tau * d;
-            mx = fmaxf(mx, logits[i]);
-        }
-        if (!isinf(mx) || mx > 0.0f) {
-            float sum = 0.0f;
-#pragma unroll
-            for (int i = 0; i < kCand; ++i) {
-                wts[i] = expf(logits[i] - mx);
-                sum += wts[i];
-            }
-            float inv_sum = 1.0f / fmaxf(sum, 1e-8f);
-#pragma unroll
-            for (int i = 0; i < kCand; ++i) {
-                wts[i] *= inv_sum;
-                if (blend >> i & 1u) {
-                    pred.x += wts[i] * cols[i].x;
-                    pred.y += wts[i] * cols[i].y;
-                    pred.z += wts[i] * cols[i].z;
-                }
-            }
-            const float* t = prm.target + 3 * pix;
-            float3 tgt = make_float3(__ldg(t), __ldg(t + 1), __ldg(t + 2));
-            dLdp = make_float3(2.0f * (pred.x - tgt.x), 2.0f * (pred.y - tgt.y),
-                               2.0f * (pred.z - tgt.z));
-            if constexpr (kSSIM) {
-                float ds = ssim_dloss(prm.rendered, prm.target, x, y, w, h);
-                float k = -prm.ssim_weight * ds;
-                dLdp.x += k * 0.299f;
-                dLdp.y += k * 0.587f;
-                dLdp.z += k * 0.114f;
-            }
-            if constexpr (kRemoval) {
-                // first slot of each distinct valid site carries its removal delta
-#pragma unroll
-                for (int i = 0; i < kCand; ++i) {
-                    if (!(valid >> i & 1u)) continue;
-                    bool first = true;
-#pragma unroll
-                    for (int j = 0; j < i; ++j) first &= !((valid >> j & 1u) && ids[j] == ids[i]);
-                    if (!first) continue;
-                    float wt = 0.0f;
-#pragma unroll
-                    for (int j = i; j < kCand; ++j)
-                        if ((valid >> j & 1u) && ids[j] == ids[i]) wt += wts[j];
-                    if (!(wt > 0.0f)) continue;
-                    float keep = 1.0f - wt;
-                    float delta;
-                    if (keep < 1e-4f) {
-                        delta = kRemovalSentinel;
-                    } else {
-                        float3 c = cols[i];
-                        float3 pk = make_float3((pred.x - wt * c.x) / keep, (pred.y - wt * c.y) / keep,
-                                                (pred.z - wt * c.z) / keep);
-                        float3 df = make_float3(pred.x - tgt.x, pred.y - tgt.y, pred.z - tgt.z);
-                        float3 dk = make_float3(pk.x - tgt.x, pk.y - tgt.y, pk.z - tgt.z);
-                        delta = (dk.x * dk.x + dk.y * dk.y + dk.z * dk.z) -
-                                (df.x * df.x + df.y * df.y + df.z * df.z);
-                    }
-                    rem[i] = delta;
-                }
-            }
-        } else {
-            valid = 0;
-        }
+        const float* t = prm.target + 3 * pix;
+        float3 tgt = make_float3(__ldg(t), __ldg(t + 1), __ldg(t + 2));
+        pixel_forward<kRemoval, kSSIM>(prm, x, y, ux, uy, inv_s2, inv_scale, ids, tgt,
+                                       [&](int i, SiteGeom& g, float3& c) { src.load(ids[i], g, c); },
+                                       wts, rem, valid, pred, dLdp);
     }
 
-    // 1. table index of every candidate: precomputed, or one CAS per (warp, site)
+    // 1. registration: one CAS per (warp, site)
     int slots[kCand];
-    if constexpr (kPre) {
 #pragma unroll
-        for (int i = 0; i < kCand; ++i) slots[i] = (valid >> i & 1u) ? pre(i) : -1;
-    } else {
-#pragma unroll
-        for (int i = 0; i < kCand; ++i)
-            slots[i] = register_key(table, (valid >> i & 1u) ? ids[i] : kEmpty);
-    }
+    for (int i = 0; i < kCand; ++i)
+        slots[i] = register_key(table, (valid >> i & 1u) ? ids[i] : kEmpty);
 
     // 2. accumulate in a lane-rotated candidate order; the loop is kept rolled (the arrays
     // shift down one entry per step) so the kernel body stays small in the instruction cache
@@ -319,24 +314,10 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
         if (vr & 1u) {
             SiteGeom g;
             float3 col;
-            if constexpr (kPre)
-                staged_site(sm, src, ids[0], slots[0], g, col);
-            else
-                src.load(ids[0], g, col);
-            float o[10];
-            candidate_grads(g, col, ux, uy, inv_s2, inv_scale, wts[0], dLdp, pred, true, o);
+            src.load(ids[0], g, col);
             float v[NV];
-#pragma unroll
-            for (int k = 0; k < 10; ++k) v[k] = o[k];
-            if constexpr (kRemoval) {
-                if constexpr (kFix) {
-                    bool sentinel = rem[0] == kRemovalSentinel;
-                    v[10] = sentinel ? 0.0f : rem[0] * prm.removal_fix_mul;
-                    v[11] = sentinel ? kFixInvScale : 0.0f;  // adds exactly 1
-                } else {
-                    v[10] = rem[0];
-                }
-            }
+            candidate_values<kFix, NV>(g, col, ux, uy, inv_s2, inv_scale, wts[0], dLdp, pred, rem[0],
+                                       prm.removal_fix_mul, v);
             if (slots[0] >= 0)
                 table.add(slots[0], v);
             else
@@ -353,6 +334,119 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
     for (int d = tid; d < used; d += 256) flush_slot<kFix, NV>(prm, table, d);
 }
 
+// Trainer form with the candidate field's registration precomputed (register_tiles_kernel):
+// the tile's keys are known before the first pixel is touched, so their values are
+// cleared and their sites staged in shared memory in one pass, and the accumulation loop
+// reads each candidate's table index, weight and site data by index instead of carrying
+// rotated register arrays.
+template <class Src, bool kRemoval, bool kSSIM>
+__global__ void __launch_bounds__(256, 3) fused_gradients_pre_kernel(GradParams prm, Src src) {
+    using L = GradLayout<true, kRemoval>;
+    constexpr int NV = L::NV;
+    auto& sm = shared_table<typename L::Pre>();
+    const int tid = threadIdx.x;
+    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int used = prm.tile_count[tile];
+    {
+        const uint32_t* keys = prm.tile_keys + static_cast<size_t>(tile) * kTileKeys;
+        for (int d = tid; d < used; d += 256) {
+            const uint32_t key = keys[d];
+            sm.dkey[d] = key;
+            sm.vals.zero(d);
+            SiteGeom g;
+            float3 c;
+            src.load(key, g, c);
+            sm.g0[d] = make_float4(g.px, g.py, g.tau, g.radius);
+            sm.g1[d] = make_float4(g.dx, g.dy, g.l1, g.l2);
+            sm.col[d] = make_float4(c.x, c.y, c.z, 0.0f);
+        }
+    }
+    __syncthreads();
+
+    const int lane = tid & 31, warp = tid >> 5;
+    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    const int y = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+    const int w = prm.width, h = prm.height;
+    const float inv_s2 = prm.inv_scale_sq;
+    const float inv_scale = sqrtf(inv_s2);
+    const float ux = static_cast<float>(x), uy = static_cast<float>(y);
+
+    // table index of each candidate, 8 x u16 packed in 4 words (0xFFFF: not in the table)
+    uint32_t pm[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    auto slot_of = [&pm](int i) {
+        uint32_t word = (i >> 1) == 0 ? pm[0] : (i >> 1) == 1 ? pm[1] : (i >> 1) == 2 ? pm[2] : pm[3];
+        uint32_t sidx = (word >> ((i & 1) << 4)) & 0xFFFFu;
+        return sidx == 0xFFFFu ? -1 : static_cast<int>(sidx);
+    };
+    auto site_at = [&](uint32_t id, int slot, SiteGeom& g, float3& c) {
+        if (slot >= 0) {
+            float4 a = sm.g0[slot], b = sm.g1[slot], q = sm.col[slot];
+            g.px = a.x; g.py = a.y; g.tau = a.z; g.radius = a.w;
+            g.dx = b.x; g.dy = b.y; g.l1 = b.z; g.l2 = b.w;
+            c = make_float3(q.x, q.y, q.z);
+        } else {
+            src.load(id, g, c);  // not in the tile's table: read directly
+        }
+    };
+
+    uint32_t valid = 0;
+    float3 pred = make_float3(0.f, 0.f, 0.f), dLdp = make_float3(0.f, 0.f, 0.f);
+    bool live = x < w && y < h;
+    const int pix = live ? y * w + x : 0;
+    int ci = 0;
+    if (live && prm.mask) live = __ldg(prm.mask + pix) > 0.0f;
+    if (live) {
+        uint4 m = __ldg(prm.slot_map + pix);
+        pm[0] = m.x; pm[1] = m.y; pm[2] = m.z; pm[3] = m.w;
+        ci = cand_index_for_pixel(x, y, w, h, prm.cand_width, prm.cand_height);
+        uint32_t ids[kCand];
+        uint4 a = __ldg(reinterpret_cast<const uint4*>(prm.cand0) + ci);
+        uint4 b = __ldg(reinterpret_cast<const uint4*>(prm.cand1) + ci);
+        ids[0] = a.x; ids[1] = a.y; ids[2] = a.z; ids[3] = a.w;
+        ids[4] = b.x; ids[5] = b.y; ids[6] = b.z; ids[7] = b.w;
+        const float* t = prm.target + 3 * pix;
+        float3 tgt = make_float3(__ldg(t), __ldg(t + 1), __ldg(t + 2));
+        float wts[kCand], rem[kCand];
+#pragma unroll
+        for (int i = 0; i < kCand; ++i) {
+            wts[i] = 0.0f;
+            rem[i] = 0.0f;
+        }
+        pixel_forward<kRemoval, kSSIM>(prm, x, y, ux, uy, inv_s2, inv_scale, ids, tgt,
+                                       [&](int i, SiteGeom& g, float3& c) { site_at(ids[i], slot_of(i), g, c); },
+                                       wts, rem, valid, pred, dLdp);
+#pragma unroll
+        for (int i = 0; i < kCand; ++i) {
+            sm.wts[i][tid] = wts[i];
+            if constexpr (kRemoval) sm.rem[i][tid] = rem[i];
+        }
+    }
+
+    // accumulate in a lane-rotated candidate order
+    const uint32_t r = lane_rotation();
+#pragma unroll 1
+    for (int j = 0; j < kCand; ++j) {
+        const int c = static_cast<int>((j + r) & 7u);
+        if (!(valid >> c & 1u)) continue;
+        const int slot = slot_of(c);
+        uint32_t id = kEmpty;
+        if (slot < 0) id = (c < 4 ? prm.cand0 : prm.cand1)[4 * static_cast<size_t>(ci) + (c & 3)];
+        SiteGeom g;
+        float3 col;
+        site_at(id, slot, g, col);
+        float v[NV];
+        candidate_values<true, NV>(g, col, ux, uy, inv_s2, inv_scale, sm.wts[c][tid], dLdp, pred,
+                                   kRemoval ? sm.rem[kRemoval ? c : 0][tid] : 0.0f,
+                                   prm.removal_fix_mul, v);
+        if (slot >= 0)
+            sm.vals.add(slot, v);
+        else
+            global_add<true, NV>(prm, id, v);
+    }
+    __syncthreads();
+    for (int d = tid; d < used; d += 256) flush_values<NV>(prm, sm.vals, sm.dkey[d], d);
+}
+
 // Tile registration of a candidate field: the table index of each (pixel, candidate)
 // and each tile's key list, with the gradient kernel's tiling (16x16 tiles, 8x4 warp
 // patches) and its registration (one CAS per warp and site).  Every candidate id below
@@ -360,7 +454,7 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
 __global__ void __launch_bounds__(256) register_tiles_kernel(const uint4* __restrict__ c0,
                                                              const uint4* __restrict__ c1, uint32_t n,
                                                              int w, int h, int cw, int ch, TileMap map) {
-    __shared__ KeyTable<kTileKeys> table;
+    __shared__ KeyTable<512> table;
     const int tid = threadIdx.x;
     table.init_keys(tid, 256);
     __syncthreads();
@@ -382,14 +476,14 @@ __global__ void __launch_bounds__(256) register_tiles_kernel(const uint4* __rest
 #pragma unroll
     for (int i = 0; i < kCand; ++i) {
         int slot = register_key(table, ids[i] < n ? ids[i] : kEmpty);
-        uint32_t sidx = slot < 0 ? 0xFFFFu : static_cast<uint32_t>(slot);
+        uint32_t sidx = (slot < 0 || slot >= kTileKeys) ? 0xFFFFu : static_cast<uint32_t>(slot);
         packed[i >> 1] |= sidx << (16 * (i & 1));
     }
     if (inside)
         map.slot_map[static_cast<size_t>(y) * w + x] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
     __syncthreads();
     const int tile = blockIdx.y * gridDim.x + blockIdx.x;
-    const int used = table.size();
+    const int used = min(table.size(), kTileKeys);
     for (int d = tid; d < used; d += 256) map.tile_keys[static_cast<size_t>(tile) * kTileKeys + d] = table.key_at(d);
     if (tid == 0) map.tile_count[tile] = used;
 }
@@ -420,12 +514,15 @@ void launch_register_tiles(const uint32_t* c0, const uint32_t* c1, uint32_t n, i
 template <class Src, bool kFix, bool kRemoval, bool kSSIM>
 static void launch_fused(const GradParams& p, Src src, cudaStream_t st) {
     dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
-    if (p.slot_map)
-        fused_gradients_kernel<Src, kFix, kRemoval, kSSIM, true>
-            <<<grid, 256, sizeof(typename GradLayout<kFix, kRemoval>::Staged), st>>>(p, src);
-    else
-        fused_gradients_kernel<Src, kFix, kRemoval, kSSIM, false>
-            <<<grid, 256, sizeof(typename GradLayout<kFix, kRemoval>::Table), st>>>(p, src);
+    if constexpr (kFix) {
+        if (p.slot_map) {
+            fused_gradients_pre_kernel<Src, kRemoval, kSSIM>
+                <<<grid, 256, sizeof(typename GradLayout<true, kRemoval>::Pre), st>>>(p, src);
+            return;
+        }
+    }
+    fused_gradients_kernel<Src, kFix, kRemoval, kSSIM>
+        <<<grid, 256, sizeof(typename GradLayout<kFix, kRemoval>::Table), st>>>(p, src);
 }
 
 cudaError_t prepare_gradient_kernels();
@@ -460,11 +557,13 @@ static void dispatch_gradients(const GradParams& p, Src src, cudaStream_t st) {
 template <class Src, bool kFix, bool kRemoval>
 static cudaError_t allow_variant() {
     size_t smem = sizeof(typename GradLayout<kFix, kRemoval>::Table);
-    size_t staged = sizeof(typename GradLayout<kFix, kRemoval>::Staged);
-    cudaError_t e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false, false>, smem);
-    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true, false>, smem);
-    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false, true>, staged);
-    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true, true>, staged);
+    cudaError_t e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, false>, smem);
+    if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_kernel<Src, kFix, kRemoval, true>, smem);
+    if constexpr (kFix) {
+        size_t pre = sizeof(typename GradLayout<true, kRemoval>::Pre);
+        if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_pre_kernel<Src, kRemoval, false>, pre);
+        if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_pre_kernel<Src, kRemoval, true>, pre);
+    }
     return e;
 }
 

@@ -91,9 +91,10 @@ struct GradParams {
     const uint32_t* tile_keys;  // [tiles][kTileKeys] keys by table index
     const int* tile_count;      // [tiles] keys in use
 };
-// Keys a 16x16 tile's accumulation table holds; the registration is precomputable because
-// it depends only on the candidate field (which changes once per VPT refresh).
-constexpr int kTileKeys = 512;
+// Keys a 16x16 tile's accumulation table holds when its registration is precomputed (the
+// registration depends only on the candidate field, which changes once per VPT refresh);
+// a tile of the 1024^2 workload holds 20-100 distinct sites, more keys go to global memory.
+constexpr int kTileKeys = 384;
 struct TileMap {
     uint4* slot_map;
     uint32_t* tile_keys;
