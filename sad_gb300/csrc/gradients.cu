@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
 // reads each candidate's table index, weight and site data by index instead of carrying
 // rotated register arrays.
 template <class Src, bool kRemoval, bool kSSIM>
-__global__ void __launch_bounds__(256, 3) fused_gradients_pre_kernel(GradParams prm, Src src) {
+__global__ void __launch_bounds__(256, 4) fused_gradients_pre_kernel(GradParams prm, Src src) {
     using L = GradLayout<true, kRemoval>;
     constexpr int NV = L::NV;
     auto& sm = shared_table<typename L::Pre>();

@@ -94,7 +94,7 @@ struct GradParams {
 // Keys a 16x16 tile's accumulation table holds when its registration is precomputed (the
 // registration depends only on the candidate field, which changes once per VPT refresh);
 // a tile of the 1024^2 workload holds 20-100 distinct sites, more keys go to global memory.
-constexpr int kTileKeys = 384;
+constexpr int kTileKeys = 320;
 struct TileMap {
     uint4* slot_map;
     uint32_t* tile_keys;
