@@ -73,6 +73,11 @@ __device__ __forceinline__ void split_fix(float v, int& h, int& l) {
     }
 }
 
+// Keys a 16x16 tile's accumulation table holds when its registration is precomputed (the
+// registration depends only on the candidate field, which changes once per VPT refresh);
+// a tile of the 1024^2 workload holds 20-100 distinct sites, more keys go to global memory.
+constexpr int kTileKeys = 320;
+
 // Accumulation modes of a tile table.
 struct AccFloat {};  // float shared atomics (order-dependent rounding, like the reference)
 struct AccSplit {};  // exact fixed point (hi, lo) words: bitwise reproducible sums
@@ -241,6 +246,32 @@ __device__ __forceinline__ uint32_t rotate_mask8(uint32_t m, uint32_t r) {
 __device__ __forceinline__ uint32_t lane_rotation() {
     uint32_t l = lane_id();
     return (l + 3u * (l >> 3)) & 7u;
+}
+
+// Registration of one pixel's candidate list into its tile's table (all 32 lanes of the
+// warp call it); writes the packed 8 x u16 table indices (0xFFFF: none) to the slot map.
+template <class Table, class Map>
+__device__ __forceinline__ void register_tile_pixel(Table& table, const uint32_t (&ids)[8],
+                                                    uint32_t n, int x, int y, int w, bool inside,
+                                                    const Map& map) {
+    uint32_t packed[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        int slot = register_key(table, ids[i] < n ? ids[i] : kEmpty);
+        uint32_t sidx = (slot < 0 || slot >= kTileKeys) ? 0xFFFFu : static_cast<uint32_t>(slot);
+        packed[i >> 1] |= sidx << (16 * (i & 1));
+    }
+    if (inside)
+        map.slot_map[static_cast<size_t>(y) * w + x] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+}
+
+// After the tile's registrations (and a barrier): its key list and count.
+template <class Table, class Map>
+__device__ __forceinline__ void write_tile_keys(const Table& table, int tid, int tile, const Map& map) {
+    const int used = min(table.size(), kTileKeys);
+    for (int d = tid; d < used; d += 256)
+        map.tile_keys[static_cast<size_t>(tile) * kTileKeys + d] = table.key_at(d);
+    if (tid == 0) map.tile_count[tile] = used;
 }
 
 #ifdef __CUDACC__

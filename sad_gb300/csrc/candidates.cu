@@ -6,6 +6,7 @@
 // the VPT pass.  The insertion rule is the reference's: a candidate already in the list
 // is skipped, otherwise it takes the first slot whose distance is strictly larger.  Lists
 // live in registers; insertion is a branch-free compare/select network.
+#include "accum.cuh"
 #include "common.cuh"
 #include "host_common.h"
 #include "kernels.h"
@@ -170,12 +171,13 @@ __device__ __forceinline__ uint32_t device_pack_jump(uint32_t idx, uint32_t pow2
 }
 
 // One VPT pass, backends/cuda/src/jfa.cu:271-386.
+// One VPT pass at candidate-field texel (x, y) (in range): writes the new list to
+// prm.out0/out1 and returns it in out.  backends/cuda/src/jfa.cu:271-386.
 template <class Src>
-__global__ void __launch_bounds__(256) vpt_kernel(VptParams prm, Src src) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    int y = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void vpt_pixel(const VptParams& prm, const Src& src, int x, int y,
+                                          uint32_t (&out)[8]) {
+
     const int w = prm.width, h = prm.height;
-    if (x >= w || y >= h) return;
     uint32_t step = prm.step, step_high = prm.step_high;
     if (prm.state) {
         uint32_t idx = prm.state->vpt_pass + prm.pass_offset;
@@ -251,6 +253,17 @@ __global__ void __launch_bounds__(256) vpt_kernel(VptParams prm, Src src) {
     }
     reinterpret_cast<uint4*>(prm.out0)[p] = make_uint4(bi[0], bi[1], bi[2], bi[3]);
     reinterpret_cast<uint4*>(prm.out1)[p] = make_uint4(bi[4], bi[5], bi[6], bi[7]);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = bi[i];
+}
+
+template <class Src>
+__global__ void __launch_bounds__(256) vpt_kernel(VptParams prm, Src src) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= prm.width || y >= prm.height) return;
+    uint32_t out[8];
+    vpt_pixel(prm, src, x, y, out);
 }
 
 static dim3 pixel_grid(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }

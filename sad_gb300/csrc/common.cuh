@@ -49,7 +49,8 @@ struct __align__(16) SiteColor {
 struct DevState {
     uint32_t iter;      // training iteration about to run
     uint32_t vpt_pass;  // global VPT pass index (jumpPassIndex of the reference)
-    uint32_t pad0, pad1;
+    float adam_c1;      // Adam bias corrections 1 / (1 - beta^t) for t = iter + 1
+    float adam_c2;
 };
 
 __device__ __forceinline__ int clampi(int x, int a, int b) { return max(a, min(b, x)); }

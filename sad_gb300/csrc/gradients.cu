@@ -472,20 +472,9 @@ __global__ void __launch_bounds__(256) register_tiles_kernel(const uint4* __rest
 #pragma unroll
         for (int i = 0; i < kCand; ++i) ids[i] = kEmpty;
     }
-    uint32_t packed[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-    for (int i = 0; i < kCand; ++i) {
-        int slot = register_key(table, ids[i] < n ? ids[i] : kEmpty);
-        uint32_t sidx = (slot < 0 || slot >= kTileKeys) ? 0xFFFFu : static_cast<uint32_t>(slot);
-        packed[i >> 1] |= sidx << (16 * (i & 1));
-    }
-    if (inside)
-        map.slot_map[static_cast<size_t>(y) * w + x] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    register_tile_pixel(table, ids, n, x, y, w, inside, map);
     __syncthreads();
-    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
-    const int used = min(table.size(), kTileKeys);
-    for (int d = tid; d < used; d += 256) map.tile_keys[static_cast<size_t>(tile) * kTileKeys + d] = table.key_at(d);
-    if (tid == 0) map.tile_count[tile] = used;
+    write_tile_keys(table, tid, blockIdx.y * gridDim.x + blockIdx.x, map);
 }
 
 size_t tile_map_words(int w, int h) {

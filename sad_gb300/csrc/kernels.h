@@ -91,10 +91,6 @@ struct GradParams {
     const uint32_t* tile_keys;  // [tiles][kTileKeys] keys by table index
     const int* tile_count;      // [tiles] keys in use
 };
-// Keys a 16x16 tile's accumulation table holds when its registration is precomputed (the
-// registration depends only on the candidate field, which changes once per VPT refresh);
-// a tile of the 1024^2 workload holds 20-100 distinct sites, more keys go to global memory.
-constexpr int kTileKeys = 320;
 struct TileMap {
     uint4* slot_map;
     uint32_t* tile_keys;
@@ -139,7 +135,10 @@ void launch_adam_train(Site* sites, float* adam, long long* fix12, const uint32_
                        const DevState* state, int iterations, uint32_t n, int w, int h,
                        cudaStream_t st);
 void launch_clear_f32(float* buf, size_t count, cudaStream_t st);
-void launch_advance_state(DevState* state, uint32_t vpt_passes, cudaStream_t st);
+// iteration counter, VPT pass counter and the next iteration's Adam bias corrections
+void launch_reset_state(DevState* state, float beta1, float beta2, cudaStream_t st);
+void launch_advance_state(DevState* state, uint32_t vpt_passes, float beta1, float beta2,
+                          cudaStream_t st);
 
 // sort.cu
 size_t radix_sort_temp_bytes(uint32_t count);

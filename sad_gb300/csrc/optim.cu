@@ -355,9 +355,7 @@ __global__ void adam_train_kernel(Site* __restrict__ sites, float* __restrict__ 
                    from_fix(q[3].x) * norm, from_fix(q[3].y) * norm, from_fix(q[4].x) * norm,
                    from_fix(q[4].y) * norm};
     Site s = site_load(sites, i);
-    float tt = static_cast<float>(state->iter + 1u);
-    float c1 = 1.0f / (1.0f - powf(hp.beta1, tt));
-    float c2 = 1.0f / (1.0f - powf(hp.beta2, tt));
+    const float c1 = state->adam_c1, c2 = state->adam_c2;
     AdamSlots a;
     adam_load(adam, i, a);
     adam_site(s, a, g, hp, c1, c2, w, h);
@@ -403,13 +401,32 @@ __global__ void clear10_kernel(SoaGrads g, uint32_t n) {
     for (int k = 0; k < 10; ++k) const_cast<float*>(g.g[k])[i] = 0.0f;
 }
 
-__global__ void advance_state_kernel(DevState* state, uint32_t vpt_passes) {
-    state->iter += 1u;
-    state->vpt_pass += vpt_passes;
+__device__ __forceinline__ void set_bias_corrections(DevState* state, float beta1, float beta2) {
+    float tt = static_cast<float>(state->iter + 1u);  // Adam step t = iter + 1
+    state->adam_c1 = 1.0f / (1.0f - powf(beta1, tt));
+    state->adam_c2 = 1.0f / (1.0f - powf(beta2, tt));
 }
 
-void launch_advance_state(DevState* state, uint32_t vpt_passes, cudaStream_t st) {
-    advance_state_kernel<<<1, 1, 0, st>>>(state, vpt_passes);
+__global__ void reset_state_kernel(DevState* state, float beta1, float beta2) {
+    state->iter = 0u;
+    state->vpt_pass = 0u;
+    set_bias_corrections(state, beta1, beta2);
+}
+
+__global__ void advance_state_kernel(DevState* state, uint32_t vpt_passes, float beta1, float beta2) {
+    state->iter += 1u;
+    state->vpt_pass += vpt_passes;
+    set_bias_corrections(state, beta1, beta2);
+}
+
+void launch_reset_state(DevState* state, float beta1, float beta2, cudaStream_t st) {
+    reset_state_kernel<<<1, 1, 0, st>>>(state, beta1, beta2);
+    note_launches(1);
+}
+
+void launch_advance_state(DevState* state, uint32_t vpt_passes, float beta1, float beta2,
+                          cudaStream_t st) {
+    advance_state_kernel<<<1, 1, 0, st>>>(state, vpt_passes, beta1, beta2);
     note_launches(1);
 }
 

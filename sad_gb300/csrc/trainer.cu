@@ -225,6 +225,8 @@ static int launch_refresh(sad_trainer* t, int src, cudaStream_t s) {
         launch_vpt_geom(p, t->vgeom, s);
         in = out;
     }
+    // the new field's tile registration (a separate pass measured faster than registering
+    // inside the VPT kernel, whose 32x8 blocks suit the gathers better)
     if (t->passes > 0)
         launch_register_tiles(t->cand0[in], t->cand1[in], t->n, t->w, t->h, t->cw, t->ch, t->tmap[in], s);
     return in;
@@ -304,7 +306,7 @@ static int iteration_body(sad_trainer* t, bool upd, bool prune, int field, int a
         launch_prune_sorted_train(t->sites, t->geom, t->pairs, t->prune_k, t->state,
                                   SAD_MAX_SPLIT_INDICES, s);
     }
-    launch_advance_state(t->state, static_cast<uint32_t>(adv_passes), s);
+    launch_advance_state(t->state, static_cast<uint32_t>(adv_passes), t->cfg.beta1, t->cfg.beta2, s);
     return next;
 }
 
@@ -580,7 +582,7 @@ extern "C" sad_status_t sad_trainer_init(sad_trainer_t* t, const float* sites_ho
                        "trainer grad clear"));
     SAD_TRY(check_cuda(cudaMemsetAsync(t->stats_fix, 0, static_cast<size_t>(t->cap) * 8 * sizeof(long long), s),
                        "trainer stats clear"));
-    SAD_TRY(check_cuda(cudaMemsetAsync(t->state, 0, sizeof(DevState), s), "trainer state clear"));
+    launch_reset_state(t->state, t->cfg.beta1, t->cfg.beta2, s);
     t->n = n0;
     t->active = active;
     t->iter = 0;
