@@ -181,6 +181,23 @@ struct TileValues<NV, N, AccSplit> {
             if (h != 0) atomicAdd(&hi[k][d], h);
         }
     }
+    // For tables where each pixel adds at most once per entry (at most 256 adds per tile
+    // entry): a candidate whose values are all below 1/4 in magnitude adds each as one
+    // word, round(v * 2^24) with |.| <= 2^22, from one fused multiply-add (adding 1.5 * 2^23
+    // rounds to an integer in the low mantissa bits) -- exactly to_fix(v); 256 such words
+    // stay below 2^30.  Larger values take the split.
+    __device__ __forceinline__ void add_unique(int d, const float (&v)[NV]) {
+        float m = 0.0f;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) m = fmaxf(m, fabsf(v[k]));
+        if (m < 0.25f) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                atomicAdd(&lo[k][d], __float_as_int(fmaf(v[k], kFixScale, 12582912.0f)) - 0x4B400000);
+        } else {
+            add(d, v);
+        }
+    }
     __device__ __forceinline__ long long fixed(int k, int d) const {
         return static_cast<long long>(hi[k][d]) * (1ll << kSplitLoBits) + static_cast<long long>(lo[k][d]);
     }
@@ -258,7 +275,12 @@ __device__ __forceinline__ void register_tile_pixel(Table& table, const uint32_t
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         int slot = register_key(table, ids[i] < n ? ids[i] : kEmpty);
-        uint32_t sidx = (slot < 0 || slot >= kTileKeys) ? 0xFFFFu : static_cast<uint32_t>(slot);
+        // a repeated id in the list takes the global path, so a pixel adds at most once
+        // to each table entry (TileValues::add_unique)
+        bool repeat = false;
+#pragma unroll
+        for (int j = 0; j < i; ++j) repeat |= ids[j] == ids[i];
+        uint32_t sidx = (slot < 0 || slot >= kTileKeys || repeat) ? 0xFFFFu : static_cast<uint32_t>(slot);
         packed[i >> 1] |= sidx << (16 * (i & 1));
     }
     if (inside)

@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(256, 4) fused_gradients_pre_kernel(GradParams 
                                    kRemoval ? sm.rem[kRemoval ? c : 0][tid] : 0.0f,
                                    prm.removal_fix_mul, v);
         if (slot >= 0)
-            sm.vals.add(slot, v);
+            sm.vals.add_unique(slot, v);
         else
             global_add<true, NV>(prm, id, v);
     }

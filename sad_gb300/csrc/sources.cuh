@@ -56,7 +56,7 @@ __device__ __forceinline__ void candidate_grads(const SiteGeom& g, float3 col, f
     float d2s = fmaxf(d2n, 1e-8f);
     float isq = rsqrtf(d2s);
     float rn = g.radius * inv_scale;
-    float dm = sqrtf(d2s) - rn;
+    float dm = d2s * isq - rn;  // sqrt(d2s) from the reciprocal root already at hand
     float gdx = l2 * dx + (l1 - l2) * g.dx * proj;
     float gdy = l2 * dy + (l1 - l2) * g.dy * proj;
     float kpos = tau * inv_s2 * isq;
