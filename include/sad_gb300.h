@@ -202,6 +202,20 @@ size_t sad_radix_sort_temp_bytes(uint32_t count);
 sad_status_t sad_radix_sort_pairs(uint32_t* pairs, uint32_t count, uint32_t max_key_exclusive,
                                   void* temp, size_t temp_bytes, sad_stream_t stream);
 
+/* The same sort without caller scratch and without allocating: its scratch is a fixed
+ * device array of the library, sized for SAD_NOALLOC_SORT_MAX_PAIRS pairs; larger counts
+ * are rejected (SAD_ERR_INVALID_ARGUMENT).  It serves hosts that must not allocate device
+ * memory on their call path: one with a fixed, pre-reserved memory budget, or a
+ * latency-bound loop in which an allocation call (which can synchronise the device) is
+ * not acceptable.  The first call on a device looks the array up (with that device
+ * current) and should come before any stream capture.  Nothing in the scratch needs to
+ * start at zero.  Overlapping calls on one device (other streams or host threads) share
+ * the scratch and race: the caller must serialise them.
+ * No counterpart in the reference (its sort always takes caller-allocated scratch). */
+#define SAD_NOALLOC_SORT_MAX_PAIRS 262144
+sad_status_t sad_radix_sort_pairs_noalloc(uint32_t* pairs, uint32_t count,
+                                          uint32_t max_key_exclusive, sad_stream_t stream);
+
 /* indices[i] = pairs[i].value for i < k.
  * replaces: launchWriteSplitIndicesFromSorted, backends/cuda/src/densify_prune.cu:395-407 */
 sad_status_t sad_write_split_indices(const uint32_t* pairs, uint32_t* indices, uint32_t k,

@@ -82,6 +82,7 @@ SIGNATURES = {
     "sad_compute_prune_score_pairs": (st, [vp, vp, vp, u32, f32, u32, vp]),
     "sad_radix_sort_temp_bytes": (sz, [u32]),
     "sad_radix_sort_pairs": (st, [vp, u32, u32, vp, sz, vp]),
+    "sad_radix_sort_pairs_noalloc": (st, [vp, u32, u32, vp]),
     "sad_write_split_indices": (st, [vp, vp, u32, vp]),
     "sad_prune_sites": (st, [vp, vp, u32, vp]),
     "sad_split_sites": (st, [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp, vp, u32, vp, i32, i32, vp]),

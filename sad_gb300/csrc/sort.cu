@@ -16,6 +16,8 @@
 #include "host_common.h"
 #include "kernels.h"
 
+#include <mutex>
+
 namespace sad {
 
 constexpr int kSortThreads = 256;
@@ -177,4 +179,60 @@ extern "C" sad_status_t sad_radix_sort_pairs(uint32_t* pairs, uint32_t count,
     SAD_REQUIRE((reinterpret_cast<uintptr_t>(temp) & 15u) == 0, "sad_radix_sort_pairs: temp must be 16-byte aligned");
     launch_radix_sort(pairs, count, max_key_exclusive, temp, as_stream(stream));
     return check_launch("sad_radix_sort_pairs");
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point: the sort's scratch is a fixed file-scope device array,
+// sized for SAD_NOALLOC_SORT_MAX_PAIRS pairs.  Its address is fetched once per device
+// with cudaGetSymbolAddress (the first call on a device does it, with that device
+// current); host code never uses the symbol itself as a device address.  Nothing in the
+// scratch has to start at zero: each pass writes the histograms and the ping-pong buffer
+// before reading them.  The scratch is shared: calls that overlap on one device (other
+// streams or host threads) race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+namespace sad {
+
+constexpr uint32_t kNoAllocMaxPairs = SAD_NOALLOC_SORT_MAX_PAIRS;
+constexpr size_t kNoAllocScratchBytes =
+    ((static_cast<size_t>(kNoAllocMaxPairs) * 8 + 255) & ~size_t(255)) +
+    ((static_cast<size_t>(256) * ((kNoAllocMaxPairs + kSortTile - 1) / kSortTile) * 4 + 255) & ~size_t(255)) +
+    256;
+
+static __device__ __align__(256) unsigned char g_noalloc_sort_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_scratch[64];
+
+static sad_status_t noalloc_scratch(void** out) {
+    int dev = 0;
+    SAD_TRY(check_cuda(cudaGetDevice(&dev), "sad_radix_sort_pairs_noalloc: cudaGetDevice"));
+    if (dev < 0 || dev >= 64)
+        return fail(SAD_ERR_UNSUPPORTED, "sad_radix_sort_pairs_noalloc: device ordinal out of range (>= 64)");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_scratch[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sort_scratch);
+        if (e != cudaSuccess) return check_cuda(e, "sad_radix_sort_pairs_noalloc: cudaGetSymbolAddress");
+        g_noalloc_scratch[dev] = p;
+    }
+    *out = g_noalloc_scratch[dev];
+    return SAD_OK;
+}
+
+}  // namespace sad
+
+extern "C" sad_status_t sad_radix_sort_pairs_noalloc(uint32_t* pairs, uint32_t count,
+                                                     uint32_t max_key_exclusive, sad_stream_t stream) {
+    clear_error();
+    SAD_REQUIRE(count == 0 || pairs, "sad_radix_sort_pairs_noalloc: null pairs");
+    SAD_REQUIRE(count <= kNoAllocMaxPairs,
+                "sad_radix_sort_pairs_noalloc: count exceeds the fixed scratch of "
+                "SAD_NOALLOC_SORT_MAX_PAIRS (262144) pairs; use sad_radix_sort_pairs");
+    SAD_REQUIRE((reinterpret_cast<uintptr_t>(pairs) & 7u) == 0,
+                "sad_radix_sort_pairs_noalloc: pairs must be 8-byte aligned");
+    if (count <= 1) return SAD_OK;
+    void* scratch = nullptr;
+    SAD_TRY(noalloc_scratch(&scratch));
+    launch_radix_sort(pairs, count, max_key_exclusive, scratch, as_stream(stream));
+    return check_launch("sad_radix_sort_pairs_noalloc");
 }
