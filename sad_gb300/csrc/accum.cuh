@@ -76,7 +76,7 @@ __device__ __forceinline__ void split_fix(float v, int& h, int& l) {
 // Keys a 16x16 tile's accumulation table holds when its registration is precomputed (the
 // registration depends only on the candidate field, which changes once per VPT refresh);
 // a tile of the 1024^2 workload holds 20-100 distinct sites, more keys go to global memory.
-constexpr int kTileKeys = 320;
+constexpr int kTileKeys = 256;
 
 // Accumulation modes of a tile table.
 struct AccFloat {};  // float shared atomics (order-dependent rounding, like the reference)
@@ -203,6 +203,52 @@ struct TileValues<NV, N, AccSplit> {
     }
 };
 
+// Fixed-point values with the lo words privatised per lane group: lanes of different
+// groups that reach the same entry at the same instruction hit different words, and the
+// copies are offset by 16 words so those words sit in different banks.  Adds follow
+// TileValues<.., AccSplit>::add_unique (at most one add per pixel and entry); the hi words
+// (rare) are shared.
+template <int NV, int N, int COPIES>
+struct PrivatisedValues {
+    static constexpr int kStride = NV * N + 16;
+    int lo[COPIES * kStride];
+    int hi[NV][N];
+
+    __device__ __forceinline__ void zero(int d) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            hi[k][d] = 0;
+#pragma unroll
+            for (int c = 0; c < COPIES; ++c) lo[c * kStride + k * N + d] = 0;
+        }
+    }
+    __device__ __forceinline__ void add_unique(int d, const float (&v)[NV], int copy) {
+        int* lc = lo + copy * kStride + d;
+        float m = 0.0f;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) m = fmaxf(m, fabsf(v[k]));
+        if (m < 0.25f) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                atomicAdd(lc + k * N, __float_as_int(fmaf(v[k], kFixScale, 12582912.0f)) - 0x4B400000);
+        } else {
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                int h, l;
+                split_fix(v[k], h, l);
+                atomicAdd(lc + k * N, l);
+                if (h != 0) atomicAdd(&hi[k][d], h);
+            }
+        }
+    }
+    __device__ __forceinline__ long long fixed(int k, int d) const {
+        long long x = static_cast<long long>(hi[k][d]) * (1ll << kSplitLoBits);
+#pragma unroll
+        for (int c = 0; c < COPIES; ++c) x += static_cast<long long>(lo[c * kStride + k * N + d]);
+        return x;
+    }
+};
+
 // Keys and values of one tile (keys registered in the kernel).
 template <int NV, int SLOTS, class Mode>
 struct TileTable : KeyTable<SLOTS>, TileValues<NV, SLOTS, Mode> {
@@ -259,10 +305,11 @@ __device__ __forceinline__ uint32_t rotate_mask8(uint32_t m, uint32_t r) {
     return ((m >> r) | (m << (8 - r))) & 0xffu;
 }
 
-// Per-lane rotation for 8x4 warp patches: lanes that share a rotation are spread apart.
+// Per-lane rotation for 8x4 warp patches (lane = x + 8y): lanes that share a rotation
+// are spread apart, so lanes with similar candidate lists visit different sites per step.
 __device__ __forceinline__ uint32_t lane_rotation() {
     uint32_t l = lane_id();
-    return (l + 3u * (l >> 3)) & 7u;
+    return ((l & 7u) * 5u + (l >> 3) * 2u) & 7u;
 }
 
 // Registration of one pixel's candidate list into its tile's table (all 32 lanes of the

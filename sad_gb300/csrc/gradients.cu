@@ -128,7 +128,7 @@ struct GradLayout {
     // precomputed registration (trainer): the tile's values, keys and staged sites, and
     // each thread's candidate weights (and removal deltas) for the accumulation loop
     struct Pre {
-        TileValues<NV, kTileKeys, Mode> vals;
+        PrivatisedValues<NV, kTileKeys, 2> vals;  // lo words per pixel-row parity
         uint32_t dkey[kTileKeys];
         float4 g0[kTileKeys];  // px, py, tau, radius
         float4 g1[kTileKeys];  // dx, dy, l1, l2
@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(256, 4) fused_gradients_pre_kernel(GradParams 
                                    kRemoval ? sm.rem[kRemoval ? c : 0][tid] : 0.0f,
                                    prm.removal_fix_mul, v);
         if (slot >= 0)
-            sm.vals.add_unique(slot, v);
+            sm.vals.add_unique(slot, v, (lane >> 3) & 1);
         else
             global_add<true, NV>(prm, id, v);
     }
