@@ -445,11 +445,13 @@ void launch_site_stats(const uint32_t* c0, const uint32_t* c1, const float* targ
     note_launches(1);
 }
 
-// Power-of-two pre-scale (<= 1) keeping a fixed-point value exact: a tile's sum below
-// 2^27 (the split shared words, 256 pixel terms of at most per_pixel each) and a site's
-// total below 2^39 (the 64-bit record, npix terms).
+// Power-of-two pre-scale keeping a fixed-point value exact with the most fractional bits:
+// the largest mul (up to 2^30) with a tile's sum below 2^27 (the split shared words, 256
+// pixel terms of at most per_pixel each) and a site's total below 2^39 (the 64-bit record,
+// npix terms).  Values far below 1 (removal deltas, weights) so keep a resolution far finer
+// than the 2^-24 of an unscaled term.
 static float fix_mul_for_bound(double per_pixel, double npix) {
-    float mul = 1.0f;
+    float mul = 0x1p30f;
     while (mul > 0x1p-60f &&
            (256.0 * per_pixel * mul >= 0x1p27 || npix * per_pixel * mul >= 0x1p39))
         mul *= 0.5f;
@@ -457,8 +459,8 @@ static float fix_mul_for_bound(double per_pixel, double npix) {
 }
 
 float removal_fix_mul(int w, int h) {
-    // per pixel |delta| <= 2^10 (squared colour errors of 3 channels)
-    return fix_mul_for_bound(1024.0, static_cast<double>(w) * h);
+    // per pixel |delta| <= 3: a difference of two squared colour errors, colours in [0, 1]
+    return fix_mul_for_bound(4.0, static_cast<double>(w) * h);
 }
 
 void launch_site_stats_fixed(const uint32_t* c0, const uint32_t* c1, const float* target,
@@ -470,7 +472,8 @@ void launch_site_stats_fixed(const uint32_t* c0, const uint32_t* c1, const float
     o.fix = fix;
     o.stride = stride;
     const double np = static_cast<double>(w) * h, fw = w, fh = h;
-    const double per_pixel[8] = {1.0, 1024.0, 1.0, fw, fh, fw * fw, fw * fh, fh * fh};
+    // weights <= 1, squared colour errors <= 3, positions below the image size
+    const double per_pixel[8] = {1.0, 4.0, 1.0, fw, fh, fw * fw, fw * fh, fh * fh};
     for (int k = 0; k < 8; ++k) o.mul[k] = fix_mul_for_bound(per_pixel[k], np);
     site_stats_kernel<true><<<stats_grid(w, h), dim3(32, 8), sizeof(TileTable<8, kStatSlots, AccSplit>), st>>>(
         reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), target, mask,
