@@ -340,6 +340,8 @@ typedef struct {
     float ssim_weight;             /* --ssim-weight */
     int log_freq;                  /* --log-freq (0: no intermediate logs) */
     int use_graphs;                /* replay each iteration kind from a CUDA graph */
+    int init_per_pixel;            /* --init-per-pixel: sites given one per pixel, candidates
+                                      initialised per pixel (launchInitCandidates' flag) */
 } sad_train_config_t;
 
 /* Fill with the reference's training_config.json values. */

@@ -38,6 +38,7 @@ class TrainConfig(C.Structure):
         ("lr_aniso", f32), ("lr_scale", f32), ("init_log_tau", f32), ("init_radius", f32),
         ("init_gradient_alpha", f32), ("beta1", f32), ("beta2", f32), ("eps", f32),
         ("ssim_weight", f32), ("log_freq", i32), ("use_graphs", i32),
+        ("init_per_pixel", i32),
     ]
 
 

@@ -2,7 +2,8 @@
 
     python -m sad_gb300.build [--force] [--verbose]
 
-Translation units compile in parallel; the shared library lands in sad_gb300/_lib/.
+Translation units compile in parallel; the shared library and the sad_cuda command-line
+host (sad_gb300/cli) land in sad_gb300/_lib/.
 Nothing here needs a GPU (nvcc cross-compiles), and no torch headers are involved:
 the boundary is the plain C ABI of include/sad_gb300.h.
 """
@@ -86,7 +87,34 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
         tmp = lib + ".tmp"
         run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs])
         os.replace(tmp, lib)
+    build_cli(force=force, verbose=verbose)
     return lib
+
+
+CLI_DIR = os.path.join(PKG, "cli")
+
+
+def cli_path() -> str:
+    return os.path.join(OUT_DIR, "sad_cuda")
+
+
+def build_cli(force: bool = False, verbose: bool = False) -> str:
+    """The sad_cuda-compatible command-line host (host C++ on the C ABI)."""
+    srcs = sorted(os.path.join(CLI_DIR, f) for f in os.listdir(CLI_DIR) if f.endswith(".cpp"))
+    deps = srcs + [os.path.join(CLI_DIR, f) for f in os.listdir(CLI_DIR) if f.endswith(".h")]
+    deps += [os.path.join(INCLUDE, "sad_gb300.h"), lib_path(), os.path.abspath(__file__)]
+    exe = cli_path()
+    if not force and not _stale(exe, deps):
+        return exe
+    cmd = [nvcc(), "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + CLI_DIR, *srcs, "-o", exe + ".tmp",
+           "-L" + OUT_DIR, "-lsad_gb300", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(exe + ".tmp", exe)
+    return exe
 
 
 if __name__ == "__main__":

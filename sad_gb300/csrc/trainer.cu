@@ -588,7 +588,7 @@ extern "C" sad_status_t sad_trainer_init(sad_trainer_t* t, const float* sites_ho
     t->iter = 0;
     t->cur = 0;
     t->hilbert_ready = false;
-    launch_init_candidates(t->cand0[0], t->cand1[0], n0, 0u, 0, t->cw, t->ch, s);
+    launch_init_candidates(t->cand0[0], t->cand1[0], n0, 0u, t->cfg.init_per_pixel ? 1 : 0, t->cw, t->ch, s);
     launch_jfa_seed(t->cand0[0], t->sites, n0, t->cw, t->ch, t->ds, s);
     launch_register_tiles(t->cand0[0], t->cand1[0], n0, t->w, t->h, t->cw, t->ch, t->tmap[0], s);
     make_plan(t);
