@@ -425,6 +425,61 @@ sad_status_t sad_render_from_sites(const sad_render_config_t* cfg, const float* 
                                    uint32_t site_count, int width, int height, float* out_rgb,
                                    void* scratch, size_t scratch_bytes, sad_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* 16-byte quantised inference sites (the Metal backend's serving format)     */
+/* ------------------------------------------------------------------------ */
+
+/* One packed site is four u32 words:
+ *   w0  x as unorm15 of [0, W-1] | y as unorm15 of [0, H-1] << 15 | inactive << 30
+ *   w1  r unorm11 | g unorm11 << 11 | b unorm10 << 22, over the ranges below
+ *   w2  log_tau unorm16 | radius unorm16 << 16, over the ranges below
+ *   w3  direction angle atan2(dy, dx) as unorm16 of [-pi, pi] | log_aniso as f16 << 16
+ * Ranges (min, scale = max(max - min, 1e-6)) are over the active sites' finite values.
+ * format: backends/metal/sources/utils/packed_inference.swift:3-18, 164-196 */
+typedef struct {
+    float log_tau_min, log_tau_scale;
+    float radius_min, radius_scale;
+    float r_min, r_scale;
+    float g_min, g_scale;
+    float b_min, b_scale;
+} sad_packed_quant_t;
+
+/* Pack site_count sites ([n,10] f32, device) into packed ([n][4] u32, device); quant
+ * (device) receives the ranges.  Inactive sites (x < 0 or y < 0) keep their slot with the
+ * inactive bit set.  Sides above 32768 are rejected (15-bit positions).
+ * replaces: makePackedInferenceSites, backends/metal/sources/utils/packed_inference.swift:86-199 */
+sad_status_t sad_pack_inference_sites(const float* sites, uint32_t site_count, int width, int height,
+                                      uint32_t* packed, sad_packed_quant_t* quant, sad_stream_t stream);
+
+/* Decode packed sites (device) to [n,10] f32 (device); inactive sites come out at
+ * position (-1, -1).
+ * replaces: decodePackedSite, backends/metal/shaders/sad_common.metal:89-120 */
+sad_status_t sad_unpack_inference_sites(const uint32_t* packed, const sad_packed_quant_t* quant,
+                                        uint32_t site_count, int width, int height, float* sites,
+                                        sad_stream_t stream);
+
+/* Render packed sites over a given candidate field (same softmax-over-8 as sad_render).
+ * replaces: renderVoronoiPacked, backends/metal/shaders/encoders/packed_render_encoder.metal:3-31 */
+sad_status_t sad_render_packed(const uint32_t* cand0, const uint32_t* cand1, float* out_rgb,
+                               const uint32_t* packed, const sad_packed_quant_t* quant,
+                               float inv_scale_sq, uint32_t site_count, int width, int height,
+                               int cand_width, int cand_height, sad_stream_t stream);
+
+/* Build the candidate field from packed sites and render them (render mode with packed
+ * sites); scratch is sad_render_packed_scratch_bytes().
+ * replaces: renderPackedInference, backends/metal/sources/rendering/packed_renderer.swift:15-135 */
+size_t sad_render_packed_scratch_bytes(uint32_t site_count, int width, int height, int cand_downscale);
+sad_status_t sad_render_packed_from_sites(const sad_render_config_t* cfg, const uint32_t* packed,
+                                          const sad_packed_quant_t* quant, uint32_t site_count,
+                                          int width, int height, float* out_rgb, void* scratch,
+                                          size_t scratch_bytes, sad_stream_t stream);
+
+/* Pack the trainer's sites and render them with its current candidate field; rgb_out and
+ * psnr_out as in sad_trainer_render.  quant_out (nullable, host) receives the ranges.
+ * replaces: the --packed-psnr re-render, backends/metal/sources/training/training.swift:676-705 */
+sad_status_t sad_trainer_render_packed(sad_trainer_t* t, float* rgb_out, float* psnr_out,
+                                       sad_packed_quant_t* quant_out);
+
 #ifdef __cplusplus
 }
 #endif

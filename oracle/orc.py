@@ -389,3 +389,21 @@ def fit_config_from(train_cfg, threads=0) -> FitConfig:
     c.init_log_tau, c.init_radius = train_cfg.init_log_tau, train_cfg.init_radius
     c.threads = threads
     return c
+
+
+def pack_inference_sites(sites, w, h):
+    """16-byte quantised sites: (packed [N,4] u32, quant [10] f32)."""
+    sites = _c(sites, np.float32)
+    n = sites.shape[0]
+    packed = np.zeros((n, 4), np.uint32)
+    quant = np.zeros(10, np.float32)
+    lib().orc_pack_inference_sites(_p(sites), u32(n), i32(w), i32(h), _p(packed), _p(quant))
+    return packed, quant
+
+
+def unpack_inference_sites(packed, quant, w, h):
+    packed = _c(packed, np.uint32)
+    quant = _c(quant, np.float32)
+    out = np.zeros((packed.shape[0], 10), np.float32)
+    lib().orc_unpack_inference_sites(_p(packed), _p(quant), u32(packed.shape[0]), i32(w), i32(h), _p(out))
+    return out

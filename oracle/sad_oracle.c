@@ -1247,3 +1247,103 @@ void orc_solve_target_bpp(float bpp, int w, int h, int init_sites, int max_sites
     out[2] = (float)best_sites;
     out[3] = (float)best_sites * bits / (float)(w * h);
 }
+
+/* ------------------------------------------------------------------------ */
+/* 16-byte quantised inference sites                                         */
+/* makePackedInferenceSites, backends/metal/sources/utils/packed_inference.swift:20-199;  */
+/* decodePackedSite, backends/metal/shaders/sad_common.metal:71-120.                      */
+/* Plain float arithmetic, one rounding per operation (built with -ffp-contract=off).     */
+/* ------------------------------------------------------------------------ */
+
+static uint32_t pk_unorm(float v, float minv, float scale, float levels) {
+    if (scale <= 0.0f) return 0u;
+    float n = fminf(fmaxf((v - minv) / scale, 0.0f), 1.0f);
+    return (uint32_t)(n * levels + 0.5f);
+}
+
+static uint32_t pk_unorm_max(float v, float maxv, float levels) {
+    if (maxv <= 0.0f) return 0u;
+    float n = fminf(fmaxf(v / maxv, 0.0f), 1.0f);
+    return (uint32_t)(n * levels + 0.5f);
+}
+
+static uint32_t pk_angle(float dx, float dy) {
+    float len2 = dx * dx + dy * dy;
+    float ux = 1.0f, uy = 0.0f;
+    if (!(len2 < 1.0e-8f)) {
+        float inv = 1.0f / sqrtf(len2);
+        ux = dx * inv;
+        uy = dy * inv;
+    }
+    const float pi = 3.14159265358979f;
+    float angle = atan2f(uy, ux);
+    float n = fminf(fmaxf((angle + pi) / (pi * 2.0f), 0.0f), 1.0f);
+    return (uint32_t)(n * 65535.0f + 0.5f);
+}
+
+void orc_pack_inference_sites(const orc_site* sites, uint32_t n, int width, int height,
+                              uint32_t* packed, float* quant) {
+    float mn[5], mx[5];
+    for (int f = 0; f < 5; f++) { mn[f] = INFINITY; mx[f] = -INFINITY; }
+    for (uint32_t i = 0; i < n; i++) {
+        const orc_site* s = &sites[i];
+        if (!(s->px >= 0.0f && s->py >= 0.0f)) continue;
+        float v[5] = {s->log_tau, s->radius, s->r, s->g, s->b};
+        for (int f = 0; f < 5; f++) {
+            if (!isfinite(v[f])) continue;
+            if (v[f] < mn[f]) mn[f] = v[f];
+            if (v[f] > mx[f]) mx[f] = v[f];
+        }
+    }
+    for (int f = 0; f < 5; f++) {
+        if (!isfinite(mn[f]) || !isfinite(mx[f])) { mn[f] = 0.0f; mx[f] = 0.0f; }
+        quant[2 * f] = mn[f];
+        quant[2 * f + 1] = fmaxf(mx[f] - mn[f], 1.0e-6f);
+    }
+    float max_x = (float)(width > 1 ? width - 1 : 0), max_y = (float)(height > 1 ? height - 1 : 0);
+    for (uint32_t i = 0; i < n; i++) {
+        const orc_site* s = &sites[i];
+        int active = s->px >= 0.0f && s->py >= 0.0f;
+        float x = fminf(fmaxf(s->px, 0.0f), max_x), y = fminf(fmaxf(s->py, 0.0f), max_y);
+        uint32_t w0 = pk_unorm_max(x, max_x, 32767.0f) | (pk_unorm_max(y, max_y, 32767.0f) << 15);
+        w0 = (w0 & 0x3fffffffu) | ((active ? 0u : 1u) << 30);
+        uint32_t w1 = pk_unorm(s->r, quant[4], quant[5], 2047.0f) | (pk_unorm(s->g, quant[6], quant[7], 2047.0f) << 11) |
+                      (pk_unorm(s->b, quant[8], quant[9], 1023.0f) << 22);
+        float lt = isfinite(s->log_tau) ? s->log_tau : quant[0];
+        float rd = isfinite(s->radius) ? s->radius : quant[2];
+        uint32_t w2 = pk_unorm(lt, quant[0], quant[1], 65535.0f) | (pk_unorm(rd, quant[2], quant[3], 65535.0f) << 16);
+        float la = isfinite(s->log_aniso) ? s->log_aniso : 0.0f;
+        uint32_t w3 = (pk_angle(s->dx, s->dy) & 0xffffu) | ((uint32_t)orc_f32_to_f16(la) << 16);
+        packed[4 * i + 0] = w0;
+        packed[4 * i + 1] = w1;
+        packed[4 * i + 2] = w2;
+        packed[4 * i + 3] = w3;
+    }
+}
+
+static float pk_unpack(uint32_t v, float inv_levels, float minv, float scale) {
+    return minv + ((float)v * inv_levels) * fmaxf(scale, 0.0f);
+}
+
+void orc_unpack_inference_sites(const uint32_t* packed, const float* quant, uint32_t n, int width, int height,
+                                orc_site* sites) {
+    const float inv16 = 1.0f / 65535.0f, inv15 = 1.0f / 32767.0f, inv11 = 1.0f / 2047.0f, inv10 = 1.0f / 1023.0f;
+    const float pi = 3.14159265f, two_pi = 6.2831853f;
+    float dim_x = (float)(width - 1), dim_y = (float)(height - 1);
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t* w = packed + 4 * i;
+        orc_site* s = &sites[i];
+        s->px = ((float)(w[0] & 0x7fffu) * inv15) * fmaxf(dim_x, 0.0f);
+        s->py = ((float)((w[0] >> 15) & 0x7fffu) * inv15) * fmaxf(dim_y, 0.0f);
+        s->r = pk_unpack(w[1] & 0x7ffu, inv11, quant[4], quant[5]);
+        s->g = pk_unpack((w[1] >> 11) & 0x7ffu, inv11, quant[6], quant[7]);
+        s->b = pk_unpack((w[1] >> 22) & 0x3ffu, inv10, quant[8], quant[9]);
+        s->log_tau = pk_unpack(w[2] & 0xffffu, inv16, quant[0], quant[1]);
+        s->radius = pk_unpack(w[2] >> 16, inv16, quant[2], quant[3]);
+        float angle = ((float)(w[3] & 0xffffu) * inv16) * two_pi - pi;
+        s->dx = cosf(angle);
+        s->dy = sinf(angle);
+        s->log_aniso = orc_f16_to_f32((uint16_t)(w[3] >> 16));
+        if ((w[0] >> 30) & 1u) s->px = s->py = -1.0f;
+    }
+}

@@ -173,6 +173,13 @@ int orc_fit_sites(orc_fit* f, orc_site* out, int capacity, int active_only);
 void orc_fit_destroy(orc_fit* f);
 void orc_set_threads(int n);
 
+/* 16-byte quantised inference sites: packed [n][4] u32, quant the 10 range floats
+ * (log_tau min/scale, radius min/scale, r, g, b min/scale). */
+void orc_pack_inference_sites(const orc_site* sites, uint32_t n, int width, int height,
+                              uint32_t* packed, float* quant);
+void orc_unpack_inference_sites(const uint32_t* packed, const float* quant, uint32_t n, int width,
+                                int height, orc_site* sites);
+
 #ifdef __cplusplus
 }
 #endif

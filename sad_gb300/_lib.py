@@ -116,6 +116,12 @@ SIGNATURES = {
     "sad_render_config_default": (None, [C.POINTER(RenderConfig)]),
     "sad_render_scratch_bytes": (sz, [u32, i32, i32, i32]),
     "sad_render_from_sites": (st, [C.POINTER(RenderConfig), vp, u32, i32, i32, vp, vp, sz, vp]),
+    "sad_pack_inference_sites": (st, [vp, u32, i32, i32, vp, vp, vp]),
+    "sad_unpack_inference_sites": (st, [vp, vp, u32, i32, i32, vp, vp]),
+    "sad_render_packed": (st, [vp, vp, vp, vp, vp, f32, u32, i32, i32, i32, i32, vp]),
+    "sad_render_packed_scratch_bytes": (sz, [u32, i32, i32, i32]),
+    "sad_render_packed_from_sites": (st, [C.POINTER(RenderConfig), vp, vp, u32, i32, i32, vp, vp, sz, vp]),
+    "sad_trainer_render_packed": (st, [vp, vp, C.POINTER(f32), vp]),
 }
 
 STATUS = {0: "SAD_OK", 1: "SAD_ERR_INVALID_ARGUMENT", 2: "SAD_ERR_CUDA", 3: "SAD_ERR_OUT_OF_MEMORY",

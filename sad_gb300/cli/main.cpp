@@ -302,6 +302,8 @@ struct Options {
     sad_render_config_t rcfg;
     InitMode init = InitMode::Gradient;
     bool ssim_metric = false;
+    bool packed_psnr = false;     // Metal CLI --packed-psnr
+    bool render_packed = false;   // Metal CLI --render-packed
     int width = 0, height = 0, max_dim = 4096;
 };
 
@@ -340,6 +342,7 @@ void usage(const Defaults& d) {
     std::printf("  --max-sites N          Max sites (default: %d)\n", c.max_sites);
     std::printf("  --lr F                 Learning-rate scale (default: 1)\n");
     std::printf("  --ssim                 Log SSIM\n");
+    std::printf("  --packed-psnr          Re-render with the 16-byte packed sites and report PSNR\n");
     std::printf("  --ssim-weight F        SSIM weight (default: 0)\n");
     std::printf("  --log-freq N           Log frequency (default: 1000)\n\n");
     std::printf("Render options:\n");
@@ -354,6 +357,7 @@ void usage(const Defaults& d) {
     std::printf("  --render-hilbert-probes N Hilbert probes for VPT candidates (default: %u)\n", c.cand_hilbert_probes);
     std::printf("  --render-cand-inject N Candidate random injects (default: %u)\n", c.cand_inject_count);
     std::printf("  --render-target <path> Optional target image for PSNR\n");
+    std::printf("  --render-packed        Render through the 16-byte packed site format\n");
 }
 
 Options parse_args(int argc, char** argv, const Defaults& d) {
@@ -434,6 +438,8 @@ Options parse_args(int argc, char** argv, const Defaults& d) {
         else if (f == "--max-sites") c.max_sites = num_i(i, f);
         else if (f == "--lr") c.lr_scale = num_f(i, f);
         else if (f == "--ssim") o.ssim_metric = true;
+        else if (f == "--packed-psnr") o.packed_psnr = true;
+        else if (f == "--render-packed") o.render_packed = true;
         else if (f == "--ssim-weight") c.ssim_weight = num_f(i, f);
         else if (f == "--log-freq") c.log_freq = num_i(i, f);
         else if (f == "--out-dir") o.out_dir = need(i, f);
@@ -454,6 +460,7 @@ Options parse_args(int argc, char** argv, const Defaults& d) {
             std::exit(1);
         }
     }
+    if (o.render_packed && !o.render) die("Error: --render-packed is only valid in render mode");
     if (!o.render && o.image.empty()) {
         usage(d);
         std::exit(1);
@@ -622,6 +629,15 @@ int train(Options& o) {
         std::printf("Saved: %s\n", sites_path.c_str());
     else
         std::fprintf(stderr, "Failed to write sites: %s\n", sites_path.c_str());
+    if (o.packed_psnr) {
+        float packed_psnr = 0.0f;
+        check(sad_trainer_render_packed(t, d_render.p, &packed_psnr, nullptr), "sad_trainer_render_packed");
+        check_cuda(cudaMemcpy(render.data(), d_render.p, npix * 12, cudaMemcpyDeviceToHost), "download");
+        std::string packed_path = (fs::path(o.out_dir) / (stem + "_packed.png")).string();
+        if (save_render(packed_path, render, w, h))
+            std::printf("Saved: %s\n", packed_path.c_str());
+        std::printf("Packed inference PSNR: %.2f dB\n", packed_psnr);
+    }
     std::printf("Final PSNR: %.1f dB (best %.1f)\n", final_psnr, best_psnr);
     if (o.ssim_metric) std::printf("Final SSIM: %.4f (best %.4f)\n", final_ssim, best_ssim);
     std::printf("Training time: %.2f s\n", train_time);
@@ -644,14 +660,28 @@ int render(Options& o) {
     const size_t npix = static_cast<size_t>(w) * h;
     DeviceBuf<float> d_sites(ls.sites.size()), d_out(npix * 3);
     check_cuda(cudaMemcpy(d_sites.p, ls.sites.data(), ls.sites.size() * 4, cudaMemcpyHostToDevice), "upload");
-    size_t scratch_bytes = sad_render_scratch_bytes(n, w, h, o.rcfg.cand_downscale);
+    size_t scratch_bytes = o.render_packed ? sad_render_packed_scratch_bytes(n, w, h, o.rcfg.cand_downscale)
+                                           : sad_render_scratch_bytes(n, w, h, o.rcfg.cand_downscale);
     DeviceBuf<unsigned char> d_scratch(scratch_bytes);
+    DeviceBuf<uint32_t> d_packed(o.render_packed ? size_t(n) * 4 : 1);
+    DeviceBuf<sad_packed_quant_t> d_quant(1);
+    if (o.render_packed) {
+        if (w > 32768 || h > 32768) die("--render-packed: image side above 32768");
+        check(sad_pack_inference_sites(d_sites.p, n, w, h, d_packed.p, d_quant.p, nullptr),
+              "sad_pack_inference_sites");
+        std::printf("Packed inference sites: %u x 16 bytes\n", n);
+    }
     cudaEvent_t e0, e1;
     check_cuda(cudaEventCreate(&e0), "event");
     check_cuda(cudaEventCreate(&e1), "event");
     check_cuda(cudaEventRecord(e0, nullptr), "event");
-    check(sad_render_from_sites(&o.rcfg, d_sites.p, n, w, h, d_out.p, d_scratch.p, scratch_bytes, nullptr),
-          "sad_render_from_sites");
+    if (o.render_packed)
+        check(sad_render_packed_from_sites(&o.rcfg, d_packed.p, d_quant.p, n, w, h, d_out.p, d_scratch.p,
+                                           scratch_bytes, nullptr),
+              "sad_render_packed_from_sites");
+    else
+        check(sad_render_from_sites(&o.rcfg, d_sites.p, n, w, h, d_out.p, d_scratch.p, scratch_bytes, nullptr),
+              "sad_render_from_sites");
     check_cuda(cudaEventRecord(e1, nullptr), "event");
     check_cuda(cudaEventSynchronize(e1), "render");
     float ms = 0.0f;

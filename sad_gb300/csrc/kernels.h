@@ -44,6 +44,13 @@ void launch_render_raw(const uint32_t* c0, const uint32_t* c1, float* out, const
 void launch_render_prepared(const uint32_t* c0, const uint32_t* c1, float* out,
                             const SiteGeom* geom, const SiteColor* color, float inv_s2,
                             uint32_t n, int w, int h, int cw, int ch, cudaStream_t st);
+void launch_render_packed(const uint32_t* c0, const uint32_t* c1, float* out, const uint32_t* packed,
+                          const float* quant, float inv_s2, uint32_t n, int w, int h, int cw, int ch,
+                          cudaStream_t st);
+void launch_pack_inference(const Site* sites, uint32_t n, int w, int h, float* quant, uint32_t* packed,
+                           cudaStream_t st);
+void launch_unpack_inference(const uint32_t* packed, const float* quant, uint32_t n, int w, int h, Site* sites,
+                             cudaStream_t st);
 void launch_init_candidates(uint32_t* c0, uint32_t* c1, uint32_t n, uint32_t seed, int per_pixel,
                             int w, int h, cudaStream_t st);
 void launch_clear_candidates(uint32_t* c0, uint32_t* c1, int w, int h, cudaStream_t st);

@@ -43,6 +43,7 @@ __global__ void __launch_bounds__(256) render_kernel(const uint4* __restrict__ c
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
+    src.prepare();
     int p = y * w + x;
     float ux = static_cast<float>(x), uy = static_cast<float>(y);
     float inv_scale = sqrtf(inv_s2);
@@ -110,6 +111,22 @@ void launch_render_prepared(const uint32_t* c0, const uint32_t* c1, float* out,
     render_kernel<PreparedSites><<<pixel_grid(w, h), dim3(32, 8), 0, st>>>(
         reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), out,
         PreparedSites{geom, color}, inv_s2, n, w, h, cw, ch);
+    note_launches(1);
+}
+
+// renderVoronoiPacked (backends/metal/shaders/encoders/packed_render_encoder.metal:3-31):
+// the same render over 16-byte quantised sites.
+void launch_render_packed(const uint32_t* c0, const uint32_t* c1, float* out, const uint32_t* packed,
+                          const float* quant, float inv_s2, uint32_t n, int w, int h, int cw, int ch,
+                          cudaStream_t st) {
+    PackedSites src{};
+    src.p = reinterpret_cast<const uint4*>(packed);
+    src.quant = quant;
+    src.dim_x = static_cast<float>(w - 1);
+    src.dim_y = static_cast<float>(h - 1);
+    render_kernel<PackedSites><<<pixel_grid(w, h), dim3(32, 8), 0, st>>>(
+        reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), out, src, inv_s2, n, w, h,
+        cw, ch);
     note_launches(1);
 }
 

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "packed.cuh"
 
 namespace sad {
 
@@ -19,6 +20,7 @@ struct RawSites {
         c = make_float3(cc.x, cc.y, d.x);
     }
     __device__ __forceinline__ float px(uint32_t id) const { return __ldg(&s[id].px); }
+    __device__ __forceinline__ void prepare() {}
 };
 
 struct PreparedSites {
@@ -30,6 +32,25 @@ struct PreparedSites {
         col = make_float3(v.x, v.y, v.z);
     }
     __device__ __forceinline__ float px(uint32_t id) const { return __ldg(&g[id].px); }
+    __device__ __forceinline__ void prepare() {}
+};
+
+// 16-byte quantised sites (packed.cuh), decoded per candidate; an inactive site reads as
+// position (-1, -1) so it is skipped like a pruned one (packedActive,
+// backends/metal/shaders/sad_common.metal:85-87).  prepare() loads the ranges once per thread.
+struct PackedSites {
+    const uint4* p;
+    const float* quant;  // device PackedQuant
+    float dim_x, dim_y;  // W-1, H-1
+    PackedQuant q;
+    __device__ __forceinline__ void prepare() { q = load_packed_quant(quant); }
+    __device__ __forceinline__ void load(uint32_t id, SiteGeom& g, float3& c) const {
+        uint4 w = __ldg(p + id);
+        Site s = decode_packed_site(w, q, dim_x, dim_y);
+        if (!packed_active(w.x)) s.px = s.py = -1.0f;
+        g = make_geom(s.px, s.py, s.log_tau, s.radius, s.dx, s.dy, s.log_aniso);
+        c = make_float3(s.r, s.g, s.b);
+    }
 };
 
 // Per-candidate parameter gradients for dL/dpred; out in site order.  clamp_l1 selects

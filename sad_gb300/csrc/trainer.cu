@@ -87,6 +87,8 @@ struct sad_trainer {
     float* stats = nullptr;         // 8 x cap
     long long* stats_fix = nullptr;  // 8 x cap, zero between densify steps
     float* render = nullptr;
+    uint32_t* packed = nullptr;   // [cap][4] 16-byte inference sites (allocated on first use)
+    float* packed_quant = nullptr;  // sad_packed_quant_t
     long long* metric = nullptr;  // fixed-point squared-error sum (reproducible PSNR)
     uint32_t* count = nullptr;
     sad::DevState* state = nullptr;
@@ -660,11 +662,8 @@ extern "C" sad_status_t sad_trainer_run(sad_trainer_t* t, int end) {
     return SAD_OK;
 }
 
-extern "C" sad_status_t sad_trainer_render(sad_trainer_t* t, float* rgb_out, float* psnr_out) {
-    clear_error();
-    SAD_REQUIRE(t, "sad_trainer_render: null trainer");
-    launch_render_prepared(t->cand0[t->cur], t->cand1[t->cur], t->render, t->geom, t->color,
-                           t->inv_s2, t->n, t->w, t->h, t->cw, t->ch, t->st);
+// Copy-out and PSNR of the image in t->render (shared by the two render entry points).
+static sad_status_t finish_render(sad_trainer* t, float* rgb_out, float* psnr_out) {
     if (rgb_out)
         SAD_TRY(check_cuda(cudaMemcpyAsync(rgb_out, t->render, static_cast<size_t>(t->w) * t->h * 12,
                                            cudaMemcpyDeviceToDevice, t->st),
@@ -681,7 +680,44 @@ extern "C" sad_status_t sad_trainer_render(sad_trainer_t* t, float* rgb_out, flo
         float mse = sum / (std::max(1.0f, t->mask_sum) * 3.0f);
         *psnr_out = mse > 0.0f ? 20.0f * log10f(1.0f / sqrtf(mse)) : 100.0f;
     }
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_trainer_render(sad_trainer_t* t, float* rgb_out, float* psnr_out) {
+    clear_error();
+    SAD_REQUIRE(t, "sad_trainer_render: null trainer");
+    launch_render_prepared(t->cand0[t->cur], t->cand1[t->cur], t->render, t->geom, t->color,
+                           t->inv_s2, t->n, t->w, t->h, t->cw, t->ch, t->st);
+    SAD_TRY(finish_render(t, rgb_out, psnr_out));
     return check_launch("sad_trainer_render");
+}
+
+extern "C" sad_status_t sad_trainer_render_packed(sad_trainer_t* t, float* rgb_out, float* psnr_out,
+                                                  sad_packed_quant_t* quant_out) {
+    clear_error();
+    SAD_REQUIRE(t, "sad_trainer_render_packed: null trainer");
+    SAD_REQUIRE(t->w <= 32768 && t->h <= 32768, "sad_trainer_render_packed: image side above 32768");
+    if (!t->packed) {
+        void* p = nullptr;
+        void* q = nullptr;
+        SAD_TRY(check_cuda(cudaMalloc(&p, static_cast<size_t>(t->cap) * 16), "trainer packed sites"));
+        t->allocs.push_back(p);
+        SAD_TRY(check_cuda(cudaMalloc(&q, sizeof(sad_packed_quant_t)), "trainer packed ranges"));
+        t->allocs.push_back(q);
+        t->packed = static_cast<uint32_t*>(p);
+        t->packed_quant = static_cast<float*>(q);
+    }
+    launch_pack_inference(t->sites, t->n, t->w, t->h, t->packed_quant, t->packed, t->st);
+    launch_render_packed(t->cand0[t->cur], t->cand1[t->cur], t->render, t->packed, t->packed_quant, t->inv_s2,
+                         t->n, t->w, t->h, t->cw, t->ch, t->st);
+    if (quant_out) {
+        SAD_TRY(check_cuda(cudaMemcpyAsync(quant_out, t->packed_quant, sizeof(sad_packed_quant_t),
+                                           cudaMemcpyDeviceToHost, t->st),
+                           "trainer packed ranges copy"));
+        SAD_TRY(check_cuda(cudaStreamSynchronize(t->st), "trainer packed sync"));
+    }
+    SAD_TRY(finish_render(t, rgb_out, psnr_out));
+    return check_launch("sad_trainer_render_packed");
 }
 
 extern "C" sad_status_t sad_trainer_get_sites(sad_trainer_t* t, float* sites_host, int capacity,

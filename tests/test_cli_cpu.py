@@ -231,6 +231,7 @@ def test_cli_configuration_errors(sad_cuda, tmp_path):
     (["img.png", "--sites"], "Missing value for --sites"),
     (["img.png", "--iters", "many"], "Invalid integer for --iters"),
     (["a.png", "b.png"], "Unexpected argument: b.png"),
+    (["a.png", "--render-packed"], "--render-packed is only valid in render mode"),
 ])
 def test_cli_argument_errors(sad_cuda, tmp_path, args, needle):
     r = _run(sad_cuda, args, tmp_path, PACKAGED_CONFIG)

@@ -127,3 +127,20 @@ def test_run_sh_batch_mode(sad_cuda, tmp_path):
     assert len(re.findall(r"Active sites: \d+/\d+", text)) == 2
     for i in range(2):
         assert (out / f"im{i}.png").exists() and (out / f"im{i}_sites.txt").exists()
+
+
+def test_cli_packed_psnr_and_render_packed(sad_cuda, image, tmp_path):
+    out = tmp_path / "res"
+    log = _fit(sad_cuda, image, out, "--packed-psnr")
+    final = float(re.search(r"Final PSNR: ([0-9.]+)", log).group(1))
+    packed = float(re.search(r"Packed inference PSNR: ([0-9.]+) dB", log).group(1))
+    assert final - 1.5 < packed <= final + 0.1
+    assert (out / "synth_packed.png").exists()
+    txt = out / "synth_sites.txt"
+    log = _run(sad_cuda, ["--render", str(txt), "--render-packed", "--render-target", str(image),
+                          "--out", str(tmp_path / "packed_render.png")], tmp_path)
+    n = sites_io.load_sites(str(txt))[0].shape[0]
+    assert f"Packed inference sites: {n} x 16 bytes" in log
+    psnr = float(re.search(r"Render PSNR: ([0-9.]+) dB", log).group(1))
+    assert psnr > packed - 1.0
+    assert imageio.read_png(str(tmp_path / "packed_render.png")).shape == (80, 96, 3)
