@@ -349,10 +349,17 @@ void sad_train_config_default(sad_train_config_t* cfg);
 
 typedef struct sad_trainer sad_trainer_t;
 
-/* Allocates every buffer of a fit of a width x height image.  The bpp rule is applied
- * here when target_bpp > 0. */
+/* Allocates every buffer of a fit of a width x height image (one device allocation).
+ * The bpp rule is applied here when target_bpp > 0. */
 sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int width, int height,
                                 sad_trainer_t** out);
+/* Device bytes of all buffers of such a fit (0 for an invalid configuration). */
+size_t sad_trainer_memory_bytes(const sad_train_config_t* cfg, int width, int height);
+/* As sad_trainer_create, with every buffer in caller-owned device memory of at least
+ * sad_trainer_memory_bytes() bytes: no allocation.  The memory must stay valid, and be
+ * ready (any stream-ordered allocation complete), until sad_trainer_destroy returns. */
+sad_status_t sad_trainer_create_in(const sad_train_config_t* cfg, int width, int height,
+                                   void* device_memory, size_t bytes, sad_trainer_t** out);
 sad_status_t sad_trainer_destroy(sad_trainer_t* t);
 sad_stream_t sad_trainer_stream(sad_trainer_t* t);
 
@@ -479,6 +486,49 @@ sad_status_t sad_render_packed_from_sites(const sad_render_config_t* cfg, const 
  * replaces: the --packed-psnr re-render, backends/metal/sources/training/training.swift:676-705 */
 sad_status_t sad_trainer_render_packed(sad_trainer_t* t, float* rgb_out, float* psnr_out,
                                        sad_packed_quant_t* quant_out);
+
+/* ------------------------------------------------------------------------ */
+/* executor: many fits and renders in flight on one GPU                       */
+/* ------------------------------------------------------------------------ */
+
+/* Host worker threads, each with its own streams, take requests first in, first out.
+ * Every request runs in one slab from the device's stream-ordered memory pool; a request
+ * waits while the slabs of running requests plus its own exceed hbm_budget_bytes
+ * (0: no limit; a request larger than the budget runs alone).
+ * No counterpart in the reference: it fits one image per process, and its run.sh batch
+ * mode (run.sh:262-373) runs the CLI once per file. */
+typedef struct {
+    int workers;              /* default 8 */
+    size_t hbm_budget_bytes;  /* default 0 */
+} sad_executor_config_t;
+
+typedef struct {
+    sad_status_t status;
+    int sites_written;  /* fit: active sites copied to sites_host */
+    float psnr;         /* fit: final PSNR */
+    double queue_ms;    /* submission to start */
+    double run_ms;      /* start to results in host memory */
+    char message[192];  /* error text when status != SAD_OK */
+} sad_request_result_t;
+
+typedef struct sad_executor sad_executor_t;
+void sad_executor_config_default(sad_executor_config_t* cfg);
+sad_status_t sad_executor_create(const sad_executor_config_t* cfg, sad_executor_t** out);
+/* Queue a whole fit (sad_trainer_fit_host semantics).  Host buffers must stay valid until
+ * the request completes; result is written by then. */
+sad_status_t sad_executor_submit_fit(sad_executor_t* ex, const sad_train_config_t* cfg,
+                                     const float* target_host, const float* mask_host, int width,
+                                     int height, float* sites_host, int capacity,
+                                     sad_request_result_t* result, uint64_t* ticket);
+/* Queue a render from host sites ([n,10] f32) into rgb_host ([H,W,3] f32). */
+sad_status_t sad_executor_submit_render(sad_executor_t* ex, const sad_render_config_t* cfg,
+                                        const float* sites_host, uint32_t site_count, int width,
+                                        int height, float* rgb_host, sad_request_result_t* result,
+                                        uint64_t* ticket);
+sad_status_t sad_executor_wait(sad_executor_t* ex, uint64_t ticket);
+sad_status_t sad_executor_wait_all(sad_executor_t* ex);
+/* Runs what is queued, then joins the workers. */
+sad_status_t sad_executor_destroy(sad_executor_t* ex);
 
 #ifdef __cplusplus
 }

@@ -56,6 +56,15 @@ class RenderConfig(C.Structure):
                 ("cand_hilbert_probes", u32)]
 
 
+class ExecutorConfig(C.Structure):
+    _fields_ = [("workers", i32), ("hbm_budget_bytes", C.c_size_t)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", i32), ("sites_written", i32), ("psnr", f32), ("queue_ms", C.c_double),
+                ("run_ms", C.c_double), ("message", C.c_char * 192)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "sad_last_error": (C.c_char_p, []),
@@ -103,6 +112,8 @@ SIGNATURES = {
     "sad_train_config_default": (None, [C.POINTER(TrainConfig)]),
     "sad_trainer_create": (st, [C.POINTER(TrainConfig), i32, i32, C.POINTER(vp)]),
     "sad_trainer_destroy": (st, [vp]),
+    "sad_trainer_memory_bytes": (sz, [C.POINTER(TrainConfig), i32, i32]),
+    "sad_trainer_create_in": (st, [C.POINTER(TrainConfig), i32, i32, vp, sz, C.POINTER(vp)]),
     "sad_trainer_stream": (vp, [vp]),
     "sad_trainer_set_target_device": (st, [vp, vp, vp]),
     "sad_trainer_set_target_host": (st, [vp, vp, vp]),
@@ -122,6 +133,15 @@ SIGNATURES = {
     "sad_render_packed_scratch_bytes": (sz, [u32, i32, i32, i32]),
     "sad_render_packed_from_sites": (st, [C.POINTER(RenderConfig), vp, vp, u32, i32, i32, vp, vp, sz, vp]),
     "sad_trainer_render_packed": (st, [vp, vp, C.POINTER(f32), vp]),
+    "sad_executor_config_default": (None, [C.POINTER(ExecutorConfig)]),
+    "sad_executor_create": (st, [C.POINTER(ExecutorConfig), C.POINTER(vp)]),
+    "sad_executor_submit_fit": (st, [vp, C.POINTER(TrainConfig), vp, vp, i32, i32, vp, i32,
+                                     C.POINTER(RequestResult), C.POINTER(C.c_uint64)]),
+    "sad_executor_submit_render": (st, [vp, C.POINTER(RenderConfig), vp, u32, i32, i32, vp,
+                                        C.POINTER(RequestResult), C.POINTER(C.c_uint64)]),
+    "sad_executor_wait": (st, [vp, C.c_uint64]),
+    "sad_executor_wait_all": (st, [vp]),
+    "sad_executor_destroy": (st, [vp]),
 }
 
 STATUS = {0: "SAD_OK", 1: "SAD_ERR_INVALID_ARGUMENT", 2: "SAD_ERR_CUDA", 3: "SAD_ERR_OUT_OF_MEMORY",

@@ -1,0 +1,277 @@
+// executor.cpp -- many fits and renders in flight on one GPU.
+//
+// The reference fits one image per process (run.sh's batch mode runs the CLI once per
+// file, run.sh:262-373).  Small images leave most of a 152-SM GPU idle, so here a pool of
+// host worker threads, each with its own CUDA streams, runs requests concurrently:
+//   * fit: a trainer placed in one stream-ordered slab (sad_trainer_create_in), the whole
+//     schedule, sites and PSNR back to host memory;
+//   * render: sites up, candidate field + render (sad_render_from_sites), pixels back.
+// Device memory comes from the device's stream-ordered pool (cudaMallocAsync /
+// cudaFreeAsync): a request's slab is reused by later requests without a device-wide
+// synchronisation (cudaFree would wait for every stream).  Admission is first in, first
+// out, and holds a request back while the slabs in use plus its own exceed the budget.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_set>
+#include <vector>
+
+#include "host_common.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    uint64_t ticket = 0;
+    int kind = 0;  // 0 fit, 1 render
+    sad_train_config_t tcfg{};
+    sad_render_config_t rcfg{};
+    const float* target = nullptr;
+    const float* mask = nullptr;
+    const float* sites_in = nullptr;
+    uint32_t n = 0;
+    int w = 0, h = 0;
+    float* sites_out = nullptr;
+    int capacity = 0;
+    float* rgb_out = nullptr;
+    sad_request_result_t* result = nullptr;
+    size_t need = 0;
+    Clock::time_point submitted;
+};
+
+inline size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+size_t render_need(const sad_render_config_t& c, uint32_t n, int w, int h) {
+    return 256 + a256(size_t(n) * 40) + a256(size_t(w) * h * 12) +
+           sad_render_scratch_bytes(n, w, h, c.cand_downscale);
+}
+
+void set_message(sad_request_result_t* r, sad_status_t st) {
+    r->status = st;
+    if (st != SAD_OK) {
+        std::strncpy(r->message, sad_last_error(), sizeof(r->message) - 1);
+        r->message[sizeof(r->message) - 1] = '\0';
+    }
+}
+
+}  // namespace
+
+struct sad_executor {
+    int device = 0;
+    size_t budget = 0;  // 0: no limit
+    size_t in_use = 0;
+    bool stop = false;
+    uint64_t next_ticket = 1;
+    std::deque<Request> queue;
+    std::unordered_set<uint64_t> inflight;  // queued or running
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::vector<std::thread> workers;
+};
+
+namespace {
+
+sad_status_t run_fit(const Request& q, void* mem, sad_request_result_t* r) {
+    sad_trainer_t* t = nullptr;
+    SAD_TRY(sad_trainer_create_in(&q.tcfg, q.w, q.h, mem, q.need, &t));
+    int written = 0;
+    float psnr = 0.0f;
+    sad_status_t st = sad_trainer_fit_host(t, q.target, q.mask, q.sites_out, q.capacity, &written, &psnr);
+    sad_trainer_destroy(t);  // synchronises the trainer's streams
+    r->sites_written = written;
+    r->psnr = psnr;
+    return st;
+}
+
+sad_status_t run_render(const Request& q, void* mem, cudaStream_t ws) {
+    char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(mem) + 255) & ~uintptr_t(255));
+    float* sites = reinterpret_cast<float*>(p);
+    p += a256(size_t(q.n) * 40);
+    float* rgb = reinterpret_cast<float*>(p);
+    size_t npx = size_t(q.w) * q.h;
+    p += a256(npx * 12);
+    size_t scratch = sad_render_scratch_bytes(q.n, q.w, q.h, q.rcfg.cand_downscale);
+    SAD_TRY(sad::check_cuda(cudaMemcpyAsync(sites, q.sites_in, size_t(q.n) * 40, cudaMemcpyHostToDevice, ws),
+                            "executor render: sites upload"));
+    SAD_TRY(sad_render_from_sites(&q.rcfg, sites, q.n, q.w, q.h, rgb, p, scratch,
+                                  reinterpret_cast<sad_stream_t>(ws)));
+    SAD_TRY(sad::check_cuda(cudaMemcpyAsync(q.rgb_out, rgb, npx * 12, cudaMemcpyDeviceToHost, ws),
+                            "executor render: pixels download"));
+    return sad::check_cuda(cudaStreamSynchronize(ws), "executor render: sync");
+}
+
+void worker_main(sad_executor* ex) {
+    if (cudaSetDevice(ex->device) != cudaSuccess) return;
+    cudaStream_t ws = nullptr;
+    if (cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking) != cudaSuccess) return;
+    for (;;) {
+        Request q;
+        {
+            std::unique_lock<std::mutex> lock(ex->mu);
+            auto admissible = [&] {
+                if (ex->queue.empty()) return false;
+                size_t need = ex->queue.front().need;
+                return ex->budget == 0 || ex->in_use == 0 || ex->in_use + need <= ex->budget;
+            };
+            ex->cv_work.wait(lock, [&] { return admissible() || (ex->stop && ex->queue.empty()); });
+            if (ex->queue.empty()) break;  // stopped and drained
+            q = ex->queue.front();
+            ex->queue.pop_front();
+            ex->in_use += q.need;
+        }
+        sad_request_result_t* r = q.result;
+        Clock::time_point start = Clock::now();
+        r->queue_ms = std::chrono::duration<double, std::milli>(start - q.submitted).count();
+        sad::clear_error();
+        void* mem = nullptr;
+        sad_status_t st = sad::check_cuda(cudaMallocAsync(&mem, q.need, ws), "executor: slab allocation");
+        if (st == SAD_OK) st = sad::check_cuda(cudaStreamSynchronize(ws), "executor: slab allocation");
+        if (st == SAD_OK) st = q.kind == 0 ? run_fit(q, mem, r) : run_render(q, mem, ws);
+        set_message(r, st);
+        if (mem) {
+            cudaFreeAsync(mem, ws);
+            cudaStreamSynchronize(ws);
+        }
+        r->run_ms = std::chrono::duration<double, std::milli>(Clock::now() - start).count();
+        {
+            std::lock_guard<std::mutex> lock(ex->mu);
+            ex->in_use -= q.need;
+            ex->inflight.erase(q.ticket);
+        }
+        ex->cv_done.notify_all();
+        ex->cv_work.notify_all();
+    }
+    cudaStreamDestroy(ws);
+}
+
+sad_status_t enqueue(sad_executor_t* ex, Request&& q, uint64_t* ticket) {
+    {
+        std::lock_guard<std::mutex> lock(ex->mu);
+        SAD_REQUIRE(!ex->stop, "sad_executor: destroyed");
+        q.ticket = ex->next_ticket++;
+        q.submitted = Clock::now();
+        if (ticket) *ticket = q.ticket;
+        ex->inflight.insert(q.ticket);
+        ex->queue.push_back(std::move(q));
+    }
+    ex->cv_work.notify_all();
+    return SAD_OK;
+}
+
+}  // namespace
+
+extern "C" void sad_executor_config_default(sad_executor_config_t* cfg) {
+    if (!cfg) return;
+    cfg->workers = 8;
+    cfg->hbm_budget_bytes = 0;
+}
+
+extern "C" sad_status_t sad_executor_create(const sad_executor_config_t* cfg, sad_executor_t** out) {
+    sad::clear_error();
+    SAD_REQUIRE(cfg && out, "sad_executor_create: null argument");
+    SAD_REQUIRE(cfg->workers > 0 && cfg->workers <= 256, "sad_executor_create: workers must be 1..256");
+    *out = nullptr;
+    auto* ex = new sad_executor();
+    ex->budget = cfg->hbm_budget_bytes;
+    sad_status_t st = sad::check_cuda(cudaGetDevice(&ex->device), "sad_executor_create: device");
+    if (st == SAD_OK) {
+        // keep freed slabs in the pool between requests instead of returning them to the
+        // driver at every synchronisation (a process-local setting of this device's pool)
+        cudaMemPool_t pool = nullptr;
+        st = sad::check_cuda(cudaDeviceGetDefaultMemPool(&pool, ex->device), "sad_executor_create: pool");
+        uint64_t keep = ex->budget ? ex->budget : ~uint64_t(0);
+        if (st == SAD_OK)
+            st = sad::check_cuda(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep),
+                                 "sad_executor_create: pool threshold");
+    }
+    if (st != SAD_OK) {
+        delete ex;
+        return st;
+    }
+    for (int i = 0; i < cfg->workers; ++i) ex->workers.emplace_back(worker_main, ex);
+    *out = ex;
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_executor_submit_fit(sad_executor_t* ex, const sad_train_config_t* cfg,
+                                                const float* target_host, const float* mask_host, int width,
+                                                int height, float* sites_host, int capacity,
+                                                sad_request_result_t* result, uint64_t* ticket) {
+    sad::clear_error();
+    SAD_REQUIRE(ex && cfg && target_host && result, "sad_executor_submit_fit: null argument");
+    SAD_REQUIRE(capacity == 0 || sites_host, "sad_executor_submit_fit: null sites buffer");
+    size_t need = sad_trainer_memory_bytes(cfg, width, height);
+    SAD_REQUIRE(need > 0, "sad_executor_submit_fit: invalid configuration or size");
+    std::memset(result, 0, sizeof(*result));
+    Request q;
+    q.kind = 0;
+    q.tcfg = *cfg;
+    q.target = target_host;
+    q.mask = mask_host;
+    q.w = width;
+    q.h = height;
+    q.sites_out = sites_host;
+    q.capacity = capacity;
+    q.result = result;
+    q.need = need;
+    return enqueue(ex, std::move(q), ticket);
+}
+
+extern "C" sad_status_t sad_executor_submit_render(sad_executor_t* ex, const sad_render_config_t* cfg,
+                                                   const float* sites_host, uint32_t site_count, int width,
+                                                   int height, float* rgb_host, sad_request_result_t* result,
+                                                   uint64_t* ticket) {
+    sad::clear_error();
+    SAD_REQUIRE(ex && cfg && sites_host && rgb_host && result, "sad_executor_submit_render: null argument");
+    SAD_REQUIRE(site_count > 0 && width > 0 && height > 0, "sad_executor_submit_render: no sites or empty image");
+    SAD_REQUIRE(cfg->candidate_passes >= 0, "sad_executor_submit_render: negative candidate passes");
+    std::memset(result, 0, sizeof(*result));
+    Request q;
+    q.kind = 1;
+    q.rcfg = *cfg;
+    q.sites_in = sites_host;
+    q.n = site_count;
+    q.w = width;
+    q.h = height;
+    q.rgb_out = rgb_host;
+    q.result = result;
+    q.need = render_need(*cfg, site_count, width, height);
+    return enqueue(ex, std::move(q), ticket);
+}
+
+extern "C" sad_status_t sad_executor_wait(sad_executor_t* ex, uint64_t ticket) {
+    sad::clear_error();
+    SAD_REQUIRE(ex, "sad_executor_wait: null executor");
+    std::unique_lock<std::mutex> lock(ex->mu);
+    SAD_REQUIRE(ticket > 0 && ticket < ex->next_ticket, "sad_executor_wait: unknown ticket");
+    ex->cv_done.wait(lock, [&] { return ex->inflight.count(ticket) == 0; });
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_executor_wait_all(sad_executor_t* ex) {
+    sad::clear_error();
+    SAD_REQUIRE(ex, "sad_executor_wait_all: null executor");
+    std::unique_lock<std::mutex> lock(ex->mu);
+    ex->cv_done.wait(lock, [&] { return ex->inflight.empty(); });
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_executor_destroy(sad_executor_t* ex) {
+    if (!ex) return SAD_OK;
+    {
+        std::lock_guard<std::mutex> lock(ex->mu);
+        ex->stop = true;  // queued requests still run
+    }
+    ex->cv_work.notify_all();
+    for (auto& t : ex->workers) t.join();
+    delete ex;
+    return SAD_OK;
+}

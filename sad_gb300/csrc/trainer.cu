@@ -87,14 +87,16 @@ struct sad_trainer {
     float* stats = nullptr;         // 8 x cap
     long long* stats_fix = nullptr;  // 8 x cap, zero between densify steps
     float* render = nullptr;
-    uint32_t* packed = nullptr;   // [cap][4] 16-byte inference sites (allocated on first use)
+    uint32_t* packed = nullptr;   // [cap][4] 16-byte inference sites
     float* packed_quant = nullptr;  // sad_packed_quant_t
     long long* metric = nullptr;  // fixed-point squared-error sum (reproducible PSNR)
     uint32_t* count = nullptr;
     sad::DevState* state = nullptr;
     uint32_t* prune_k = nullptr;
     void* init_temp = nullptr;
-    std::vector<void*> allocs;
+    void* slab = nullptr;       // device memory of every buffer above
+    size_t slab_bytes = 0;
+    bool owns_slab = false;
 
     cudaStream_t st = nullptr, side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -110,20 +112,18 @@ struct sad_trainer {
 
 namespace sad {
 
-static sad_status_t dalloc(sad_trainer* t, void** p, size_t bytes) {
-    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
-    if (e != cudaSuccess) {
-        set_error("trainer allocation of %zu bytes: %s", bytes, cudaGetErrorString(e));
-        return e == cudaErrorMemoryAllocation ? SAD_ERR_OUT_OF_MEMORY : SAD_ERR_CUDA;
+// Every device buffer of a fit lives in one slab: offsets are planned once (base null)
+// to size it, then assigned from the slab's base.  One allocation per fit, or none when
+// the caller provides the memory (sad_trainer_create_in).
+struct SlabCarver {
+    char* base;
+    size_t off = 0;
+    template <class T>
+    void take(T*& p, size_t count) {
+        p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += (std::max<size_t>(count * sizeof(T), 16) + 255) & ~size_t(255);
     }
-    t->allocs.push_back(*p);
-    return SAD_OK;
-}
-
-template <class T>
-static sad_status_t dalloc_n(sad_trainer* t, T** p, size_t count) {
-    return dalloc(t, reinterpret_cast<void**>(p), count * sizeof(T));
-}
+};
 
 static void drop_graphs(sad_trainer* t) {
     for (auto& a : t->graphs)
@@ -369,16 +369,13 @@ static sad_status_t log_iteration(sad_trainer* t, int it) {
 
 using namespace sad;
 
-extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int width, int height,
-                                           sad_trainer_t** out) {
-    clear_error();
-    SAD_REQUIRE(cfg && out, "sad_trainer_create: null argument");
+// Sizes and schedule constants of a fit (no device work).
+static sad_status_t plan_trainer(sad_trainer* t, const sad_train_config_t* cfg, int width, int height) {
+    SAD_REQUIRE(cfg, "sad_trainer_create: null argument");
     SAD_REQUIRE(width > 0 && height > 0, "sad_trainer_create: invalid image size");
     SAD_REQUIRE(cfg->iterations >= 0, "sad_trainer_create: negative iterations");
     SAD_REQUIRE(cfg->n_sites > 0, "sad_trainer_create: n_sites must be positive");
     SAD_REQUIRE(cfg->cand_update_passes >= 0, "sad_trainer_create: negative candidate passes");
-    sad_trainer* t = new sad_trainer();
-    *out = nullptr;
     t->cfg = *cfg;
     t->w = width;
     t->h = height;
@@ -401,62 +398,72 @@ extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int wi
     if (cfg->target_bpp > 0.0f) {
         int prune_end = cfg->prune_end > 0 ? cfg->prune_end : cfg->iterations - 1;
         sad_bpp_solution_t sol{};
-        sad_status_t s = sad_solve_target_bpp(
+        SAD_TRY(sad_solve_target_bpp(
             cfg->target_bpp, width, height, cfg->n_sites, max_cap, cfg->iterations, cfg->densify,
             cfg->densify_start, cfg->densify_end, std::max(1, cfg->densify_freq),
             cfg->densify_percentile, cfg->prune_during_densify, cfg->prune_start, prune_end,
-            std::max(1, cfg->prune_freq), cfg->prune_percentile, SAD_MAX_SPLIT_INDICES, &sol);
-        if (s != SAD_OK) {
-            delete t;
-            return s;
-        }
+            std::max(1, cfg->prune_freq), cfg->prune_percentile, SAD_MAX_SPLIT_INDICES, &sol));
         t->densify_pct = sol.densify_percentile;
         t->prune_pct = sol.prune_percentile;
     }
-    size_t np = static_cast<size_t>(width) * height;
-    size_t nc = static_cast<size_t>(t->cw) * t->ch * 4;
-    uint32_t cap = t->cap;
-    t->hpadded = (cap + 1023u) / 1024u * 1024u;
-    size_t sort_bytes = radix_sort_temp_bytes(std::max(cap, t->hpadded));
-    sad_status_t s = SAD_OK;
-#define ALLOC(p, cnt)                                  \
-    if (s == SAD_OK) s = dalloc_n(t, &(p), (cnt));
-    ALLOC(t->target, np * 3);
-    ALLOC(t->mask, np);
-    ALLOC(t->sites, cap);
-    ALLOC(t->geom, cap);
-    ALLOC(t->color, cap);
-    ALLOC(t->vgeom, cap);
-    ALLOC(t->adam, static_cast<size_t>(cap) * 20);
-    ALLOC(t->grads, static_cast<size_t>(cap) * 12);
-    ALLOC(t->tau_a, cap);
-    ALLOC(t->tau_b, cap);
-    ALLOC(t->tau_nbr, static_cast<size_t>(cap) * 8);
-    ALLOC(t->tau_raw, cap);
-    ALLOC(t->tau_active, cap);
-    ALLOC(t->pairs, static_cast<size_t>(cap) * 2);
-    ALLOC(t->idx, SAD_MAX_SPLIT_INDICES);
-    for (int b = 0; b < 3; ++b) {
-        ALLOC(t->cand0[b], nc);
-        ALLOC(t->cand1[b], nc);
-        ALLOC(t->tmap_mem[b], tile_map_words(width, height));
-        if (s == SAD_OK) t->tmap[b] = tile_map_at(t->tmap_mem[b], width, height);
-    }
-    ALLOC(t->horder, cap);
-    ALLOC(t->hpos, cap);
-    ALLOC(t->hpairs, static_cast<size_t>(t->hpadded) * 2);
-    ALLOC(t->stats, static_cast<size_t>(cap) * 8);
-    ALLOC(t->stats_fix, static_cast<size_t>(cap) * 8);
-    ALLOC(t->render, np * 3);
-    ALLOC(t->metric, 1);
-    ALLOC(t->count, 4);
-    ALLOC(t->state, 1);
-    ALLOC(t->prune_k, std::max(1, cfg->iterations));
-#undef ALLOC
-    if (s == SAD_OK) s = dalloc(t, &t->sort_temp, sort_bytes);
-    if (s == SAD_OK) s = check_cuda(prepare_gradient_kernels(), "trainer kernel attributes");
+    t->hpadded = (t->cap + 1023u) / 1024u * 1024u;
     t->removal_mul = removal_fix_mul(width, height);
-    if (s == SAD_OK) s = dalloc(t, &t->init_temp, init_temp_bytes(static_cast<uint32_t>(cfg->n_sites)));
+    return SAD_OK;
+}
+
+// Assigns every buffer from base (or only sizes them when base is null); returns the
+// slab size, including 256 bytes of alignment slack.
+static size_t carve_trainer(sad_trainer* t, void* base) {
+    uintptr_t aligned = (reinterpret_cast<uintptr_t>(base) + 255) & ~uintptr_t(255);
+    SlabCarver c{base ? reinterpret_cast<char*>(aligned) : nullptr};
+    size_t np = static_cast<size_t>(t->w) * t->h;
+    size_t nc = static_cast<size_t>(t->cw) * t->ch * 4;
+    size_t cap = t->cap;
+    c.take(t->target, np * 3);
+    c.take(t->mask, np);
+    c.take(t->sites, cap);
+    c.take(t->geom, cap);
+    c.take(t->color, cap);
+    c.take(t->vgeom, cap);
+    c.take(t->adam, cap * 20);
+    c.take(t->grads, cap * 12);
+    c.take(t->tau_a, cap);
+    c.take(t->tau_b, cap);
+    c.take(t->tau_nbr, cap * 8);
+    c.take(t->tau_raw, cap);
+    c.take(t->tau_active, cap);
+    c.take(t->pairs, cap * 2);
+    c.take(t->idx, SAD_MAX_SPLIT_INDICES);
+    for (int b = 0; b < 3; ++b) {
+        c.take(t->cand0[b], nc);
+        c.take(t->cand1[b], nc);
+        c.take(t->tmap_mem[b], tile_map_words(t->w, t->h));
+        if (base) t->tmap[b] = tile_map_at(t->tmap_mem[b], t->w, t->h);
+    }
+    c.take(t->horder, cap);
+    c.take(t->hpos, cap);
+    c.take(t->hpairs, static_cast<size_t>(t->hpadded) * 2);
+    c.take(t->stats, cap * 8);
+    c.take(t->stats_fix, cap * 8);
+    c.take(t->render, np * 3);
+    c.take(t->packed, cap * 4);
+    c.take(t->packed_quant, 16);
+    c.take(t->metric, 1);
+    c.take(t->count, 4);
+    c.take(t->state, 1);
+    c.take(t->prune_k, static_cast<size_t>(std::max(1, t->cfg.iterations)));
+    char* sort_temp = nullptr;
+    c.take(sort_temp, radix_sort_temp_bytes(std::max<uint32_t>(t->cap, t->hpadded)));
+    t->sort_temp = sort_temp;
+    char* init_temp = nullptr;
+    c.take(init_temp, init_temp_bytes(static_cast<uint32_t>(t->cfg.n_sites)));
+    t->init_temp = init_temp;
+    return c.off + 256;
+}
+
+// Streams, events and kernel attributes once the buffers are in place.
+static sad_status_t finish_create(sad_trainer* t) {
+    sad_status_t s = check_cuda(prepare_gradient_kernels(), "trainer kernel attributes");
     if (s == SAD_OK)
         s = check_cuda(cudaStreamCreateWithFlags(&t->st, cudaStreamNonBlocking), "trainer stream");
     if (s == SAD_OK)
@@ -465,15 +472,65 @@ extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int wi
         s = check_cuda(cudaEventCreateWithFlags(&t->ev_fork, cudaEventDisableTiming), "trainer event");
     if (s == SAD_OK)
         s = check_cuda(cudaEventCreateWithFlags(&t->ev_join, cudaEventDisableTiming), "trainer event");
+    return s;
+}
+
+static sad_status_t create_common(const sad_train_config_t* cfg, int width, int height, void* memory,
+                                  size_t bytes, sad_trainer_t** out) {
+    clear_error();
+    SAD_REQUIRE(out, "sad_trainer_create: null argument");
+    *out = nullptr;
+    sad_trainer* t = new sad_trainer();
+    sad_status_t s = plan_trainer(t, cfg, width, height);
+    if (s != SAD_OK) {
+        delete t;
+        return s;
+    }
+    size_t need = carve_trainer(t, nullptr);
+    if (memory) {
+        if (bytes < need) {
+            delete t;
+            set_error("sad_trainer_create_in: %zu bytes given, %zu needed (sad_trainer_memory_bytes)", bytes, need);
+            return SAD_ERR_INVALID_ARGUMENT;
+        }
+        t->slab = memory;
+    } else {
+        cudaError_t e = cudaMalloc(&t->slab, need);
+        if (e != cudaSuccess) {
+            delete t;
+            set_error("trainer allocation of %zu bytes: %s", need, cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? SAD_ERR_OUT_OF_MEMORY : SAD_ERR_CUDA;
+        }
+        t->owns_slab = true;
+    }
+    t->slab_bytes = need;
+    carve_trainer(t, t->slab);
+    s = finish_create(t);
     if (s != SAD_OK) {
         std::string msg = sad_last_error();
         sad_trainer_destroy(t);
         set_error("%s", msg.c_str());
         return s;
     }
-    // all-ones mask until a target is given
     *out = t;
     return SAD_OK;
+}
+
+extern "C" size_t sad_trainer_memory_bytes(const sad_train_config_t* cfg, int width, int height) {
+    sad_trainer t;
+    if (plan_trainer(&t, cfg, width, height) != SAD_OK) return 0;
+    return carve_trainer(&t, nullptr);
+}
+
+extern "C" sad_status_t sad_trainer_create(const sad_train_config_t* cfg, int width, int height,
+                                           sad_trainer_t** out) {
+    return create_common(cfg, width, height, nullptr, 0, out);
+}
+
+extern "C" sad_status_t sad_trainer_create_in(const sad_train_config_t* cfg, int width, int height,
+                                              void* device_memory, size_t bytes, sad_trainer_t** out) {
+    SAD_REQUIRE(device_memory, "sad_trainer_create_in: null memory");
+    return create_common(cfg, width, height, device_memory, bytes, out);
 }
 
 extern "C" sad_status_t sad_trainer_destroy(sad_trainer_t* t) {
@@ -486,7 +543,7 @@ extern "C" sad_status_t sad_trainer_destroy(sad_trainer_t* t) {
     if (t->ev_join) cudaEventDestroy(t->ev_join);
     if (t->st) cudaStreamDestroy(t->st);
     if (t->side) cudaStreamDestroy(t->side);
-    for (void* p : t->allocs) cudaFree(p);
+    if (t->owns_slab && t->slab) cudaFree(t->slab);
     delete t;
     return SAD_OK;
 }
@@ -697,16 +754,6 @@ extern "C" sad_status_t sad_trainer_render_packed(sad_trainer_t* t, float* rgb_o
     clear_error();
     SAD_REQUIRE(t, "sad_trainer_render_packed: null trainer");
     SAD_REQUIRE(t->w <= 32768 && t->h <= 32768, "sad_trainer_render_packed: image side above 32768");
-    if (!t->packed) {
-        void* p = nullptr;
-        void* q = nullptr;
-        SAD_TRY(check_cuda(cudaMalloc(&p, static_cast<size_t>(t->cap) * 16), "trainer packed sites"));
-        t->allocs.push_back(p);
-        SAD_TRY(check_cuda(cudaMalloc(&q, sizeof(sad_packed_quant_t)), "trainer packed ranges"));
-        t->allocs.push_back(q);
-        t->packed = static_cast<uint32_t*>(p);
-        t->packed_quant = static_cast<float*>(q);
-    }
     launch_pack_inference(t->sites, t->n, t->w, t->h, t->packed_quant, t->packed, t->st);
     launch_render_packed(t->cand0[t->cur], t->cand1[t->cur], t->render, t->packed, t->packed_quant, t->inv_s2,
                          t->n, t->w, t->h, t->cw, t->ch, t->st);
