@@ -2,6 +2,7 @@
 schedule (128,000 sites pruned to 8,192 over 4,000 iterations), on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --workload batch|serve      (the 64-image batch and the serving mix)
 
 A step is one whole fit of the workload.  `value` is the training-loop throughput in
 iterations/s with the image already resident in HBM (init excluded, as in the
@@ -298,6 +299,179 @@ def run_reference(args):
             "note": "the reference's path is CUDA-only; this is the CPU restatement of its kernels"}
 
 
+# ---------------------------------------------------------------------------
+# batched fits (64 images of mixed sizes) and the serving mix, through the executor
+# ---------------------------------------------------------------------------
+BATCH_METRIC = "batch fit wall time, 64 images (sides log-uniform 128-2048, aspect 0.5-2), 1.0 bpp, 2000 iters"
+SERVE_METRIC = ("serving latency p99 ms: Poisson arrivals, 70% render-from-sites 256^2-4096^2 at 1 bpp, "
+                "30% fit 256^2-1024^2 x500 iters")
+
+
+def batch_specs(count: int, seed: int = 2024):
+    """(width, height, seed) of the batch images: geometric-mean side log-uniform in
+    [128, 2048], aspect ratio log-uniform in [0.5, 2]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        side = float(np.exp(rng.uniform(np.log(128.0), np.log(2048.0))))
+        aspect = float(np.exp(rng.uniform(np.log(0.5), np.log(2.0))))
+        w = int(np.clip(round(side * np.sqrt(aspect)), 64, 4096))
+        h = int(np.clip(round(side / np.sqrt(aspect)), 64, 4096))
+        out.append((w, h, seed + 1 + i))
+    return out
+
+
+def batch_images(count: int):
+    from sad_gb300.synthetic import quantize_u8, synthetic_image
+    return [quantize_u8(synthetic_image(w, h, seed=sd)) for w, h, sd in batch_specs(count)]
+
+
+def run_batch(args):
+    """All images submitted at once to the executor; the step is the whole batch."""
+    import torch
+    from sad_gb300.config import train_config
+    from sad_gb300.executor import Executor
+    torch.cuda.set_device(0)
+    imgs = batch_images(args.batch_images)
+    cfg = train_config(log_freq=0, iterations=args.batch_iters)
+    mpix_iters = sum(i.shape[0] * i.shape[1] for i in imgs) * args.batch_iters / 1e6
+
+    def run(workers):
+        with Executor(workers=workers) as ex:
+            t0 = time.perf_counter()
+            reqs = [ex.submit_fit(img, config=cfg) for img in imgs]
+            ex.wait_all()
+            wall = time.perf_counter() - t0
+            res = [r.result() for r in reqs]
+        return wall, [p for _, p in res], [len(s) for s, _ in res], [r.run_ms for r in reqs]
+
+    with Executor(workers=2) as ex:  # warm-up: kernel loading, pool growth
+        for img in imgs[:2]:
+            ex.submit_fit(img, config=train_config(log_freq=0, iterations=50))
+        ex.wait_all()
+    with ClockSampler(0) as clk:
+        walls = []
+        for _ in range(args.steps):
+            wall, psnr, sites, run_ms = run(args.workers)
+            walls.append(wall)
+    seq_wall = run(1)[0] if args.batch_sequential else None
+    wall = float(np.median(walls))
+    return {
+        "metric": BATCH_METRIC, "value": round(wall, 3), "unit": "s", "n_gpus": 1, "steps": args.steps,
+        "warmup": 1, "ms_per_step": round(1e3 * wall, 1), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded gradient + blobs + polygons per image, quantised to 8 bits",
+        "config": {"workload": f"{len(imgs)} fits, sizes {min(i.shape[1] for i in imgs)}-"
+                               f"{max(i.shape[1] for i in imgs)} wide, 1.0 bpp, {args.batch_iters} iterations "
+                               f"each, {args.workers} executor workers",
+                   "images": [f"{i.shape[1]}x{i.shape[0]}" for i in imgs]},
+        "mpix_iters_per_s": round(mpix_iters / wall, 1),
+        "images_per_s": round(len(imgs) / wall, 3),
+        "sequential_wall_s": None if seq_wall is None else round(seq_wall, 3),
+        "psnr_db_mean": round(float(np.mean(psnr)), 3), "sites_final_total": int(sum(sites)),
+        "fit_run_ms": {"p50": round(float(np.median(run_ms)), 1), "max": round(float(np.max(run_ms)), 1)},
+        "e2e": {"value": round(wall, 3), "unit": "s", "h2d_bytes_per_step": int(sum(i.nbytes for i in imgs)),
+                "d2h_bytes_per_step": int(40 * sum(sites) + 4 * len(imgs))},
+        "clocks": clk.summary(),
+    }
+
+
+def serve_requests(count: int, seed: int):
+    """Seeded request mix: 70% renders (square side log-uniform 256..4096, sites at 1 bpp),
+    30% fits (side log-uniform 256..1024, snapped to a pool of six sizes, 500 iterations)."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    pool = [256, 320, 448, 576, 768, 1024]
+    for i in range(count):
+        if rng.random() < 0.7:
+            side = int(round(np.exp(rng.uniform(np.log(256), np.log(4096)))))
+            reqs.append(("render", side, i))
+        else:
+            side = float(np.exp(rng.uniform(np.log(256), np.log(1024))))
+            reqs.append(("fit", min(pool, key=lambda p: abs(np.log(p / side))), i))
+    return reqs
+
+
+def render_sites(side: int, seed: int):
+    rng = np.random.default_rng(seed)
+    n = max(1, round(side * side / 128))
+    s = np.zeros((n, 10), np.float32)
+    s[:, 0:2] = np.floor(rng.uniform(0, side, (n, 2))) + 0.25
+    s[:, 2], s[:, 3] = 5.0, 4.0
+    s[:, 4:7] = rng.uniform(0, 1, (n, 3))
+    th = rng.uniform(0, np.pi, n)
+    s[:, 7], s[:, 8] = np.cos(th), np.sin(th)
+    s[:, 9] = np.clip(rng.normal(0, 0.42, n), -4, 4)
+    return s
+
+
+def run_serve(args):
+    import torch
+    from sad_gb300.config import train_config
+    from sad_gb300.executor import Executor
+    from sad_gb300.synthetic import quantize_u8, synthetic_image
+    torch.cuda.set_device(0)
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    fit_cfg = train_config(log_freq=0, iterations=500)
+    fit_imgs = {s: quantize_u8(synthetic_image(s, s, seed=s)) for s in (256, 320, 448, 576, 768, 1024)}
+    sites_cache = {}
+    budget = int(args.serve_budget_gb * (1 << 30))
+    rows = []
+    with Executor(workers=args.workers, hbm_budget_bytes=budget) as ex:
+        for kind, side, i in serve_requests(8, 99):  # warm-up
+            if kind == "fit":
+                ex.submit_fit(fit_imgs[side], config=train_config(log_freq=0, iterations=50))
+            else:
+                ex.submit_render(render_sites(min(side, 1024), i), min(side, 1024), min(side, 1024))
+        ex.wait_all()
+        for ri, rate in enumerate(rates):
+            reqs = serve_requests(args.serve_count, 1000 + ri)
+            gaps = np.random.default_rng(7 + ri).exponential(1.0 / rate, len(reqs))
+            subs, kinds = [], []
+            t0 = time.perf_counter()
+            due = t0
+            for (kind, side, i), gap in zip(reqs, gaps):
+                due += gap
+                delay = due - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                if kind == "fit":
+                    subs.append(ex.submit_fit(fit_imgs[side], config=fit_cfg))
+                else:
+                    if (side, i) not in sites_cache:
+                        sites_cache[(side, i)] = render_sites(side, i)
+                    subs.append(ex.submit_render(sites_cache[(side, i)], side, side))
+                kinds.append(kind)
+            ex.wait_all()
+            elapsed = time.perf_counter() - t0
+            lat = {"fit": [], "render": []}
+            for k, r in zip(kinds, subs):
+                assert r.res.status == 0, r.res.message
+                lat[k].append(r.queue_ms + r.run_ms)
+            subs.clear()
+            sites_cache.clear()
+            allv = lat["fit"] + lat["render"]
+            row = {"rate_per_s": rate, "requests": len(allv), "completed_per_s": round(len(allv) / elapsed, 2),
+                   "p50_ms": round(float(np.percentile(allv, 50)), 1),
+                   "p99_ms": round(float(np.percentile(allv, 99)), 1)}
+            for k in ("render", "fit"):
+                if lat[k]:
+                    row[f"{k}_p50_ms"] = round(float(np.percentile(lat[k], 50)), 1)
+                    row[f"{k}_p99_ms"] = round(float(np.percentile(lat[k], 99)), 1)
+            rows.append(row)
+    top = rows[-1]
+    return {
+        "metric": SERVE_METRIC, "value": top["p99_ms"], "unit": "ms", "n_gpus": 1, "steps": len(rates),
+        "warmup": 1, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: random 1-bpp site sets for renders, seeded synthetic images for fits",
+        "config": {"workload": f"{args.serve_count} requests per rate, Poisson arrivals at {rates} /s, "
+                               f"{args.workers} workers, HBM budget {args.serve_budget_gb} GB",
+                   "latency": "submission to results in host memory"},
+        "rates": rows,
+        "e2e": {"value": top["p99_ms"], "unit": "ms", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+    }
+
+
 def run_profile(args):
     """Eager (graph-free) fit of the workload for `--profile-iters` iterations, so every
     kernel is a separate launch for ncu; nothing is timed."""
@@ -325,9 +499,28 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     ap.add_argument("--profile-iters", type=int, default=200)
+    ap.add_argument("--workload", default="fit", choices=["fit", "batch", "serve"],
+                    help="fit: the 1024x1024 headline fit; batch: 64 mixed-size fits through the "
+                         "executor; serve: the Poisson render/fit mix")
+    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--batch-images", type=int, default=64)
+    ap.add_argument("--batch-iters", type=int, default=2000)
+    ap.add_argument("--batch-sequential", action="store_true", help="also time the batch with one worker")
+    ap.add_argument("--serve-rates", default="5,10,20,40")
+    ap.add_argument("--serve-count", type=int, default=60)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     args = ap.parse_args()
     if args.mode == "profile":
         run_profile(args)
+        return
+    if args.workload != "fit":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "workload": args.workload,
+                              "unavailable": "the reference fits one image per process; its batch timing "
+                                             "is oracle/ref/time_reference.py --batch"}), flush=True)
+            return
+        out = run_batch(args) if args.workload == "batch" else run_serve(args)
+        print(json.dumps(out), flush=True)
         return
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     out = run_reference(args) if args.impl == "reference" else run_ours(args)

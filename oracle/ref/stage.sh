@@ -1,6 +1,6 @@
 #!/usr/bin/env bash
 # Copy the reference's CUDA backend sources (kernels, host driver, vendored IO headers,
-# training_config.json) from the read-only reference checkout into baseline/_ref/, the
+# training_config.json) and its PyTorch extension's CUDA bindings from the read-only reference checkout into baseline/_ref/, the
 # git-ignored location for the reference that travels with the repository snapshot to the
 # GPU machine.  Nothing here is committed; oracle/ref/build.sh compiles from that copy.
 #   usage: oracle/ref/stage.sh [/path/to/reference]
@@ -13,4 +13,8 @@ mkdir -p "$DST"
 cp -r "$REF/backends/cuda/src" "$DST/src"
 cp -r "$REF/backends/cuda/third_party" "$DST/third_party"
 cp "$REF/training_config.json" "$DST/"
+# the PyTorch extension's CUDA bindings (render_sad / render_sad_backward and the rest)
+mkdir -p "$DST/torch_ext"
+cp "$REF/backends/pytorch/torch_ext/torch_binding.cpp" "$REF/backends/pytorch/torch_ext/torch_binding.h" "$DST/torch_ext/"
+cp -r "$REF/backends/pytorch/torch_ext/cuda" "$DST/torch_ext/cuda"
 echo "staged $(ls "$DST/src" | wc -l) files into $DST"

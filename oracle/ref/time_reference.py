@@ -3,6 +3,7 @@ the identical 8-bit image (equal-PSNR speed comparison).  Prints one JSON line.
 
     oracle/ref/stage.sh /path/to/reference && oracle/ref/build.sh
     python oracle/ref/time_reference.py [--repeats 2] [--size 1024] [--seeds 4]
+    python oracle/ref/time_reference.py --batch 64 [--iters 2000] [--workers 8]
 
 The reference binary (oracle/_ref/sad_cuda, built from the staged copy of its sources)
 reads training_config.json from its working directory (baseline/_ref/sad holds the staged
@@ -78,13 +79,62 @@ def run_ours(img, repeats: int):
     return best
 
 
+def run_batch(count: int, iters: int, workers: int):
+    """The batch workload (bench.py --workload batch): the reference CLI once per image,
+    sequentially (its run.sh batch mode), against this library's executor on the same
+    8-bit images and iteration count."""
+    import bench
+    from sad_gb300 import imageio
+    from sad_gb300.config import train_config
+    from sad_gb300.executor import Executor
+    exe = os.path.join(ROOT, "oracle", "_ref", "sad_cuda")
+    cwd = os.path.join(ROOT, "baseline", "_ref", "sad")
+    imgs = bench.batch_images(count)
+    d = tempfile.mkdtemp()
+    pngs = []
+    for k, img in enumerate(imgs):
+        pngs.append(os.path.join(d, f"batch_{k:02d}.png"))
+        imageio.save_image(pngs[-1], img)
+    ref_psnr = []
+    t0 = time.perf_counter()
+    for png in pngs:
+        r = subprocess.run([exe, png, "--iters", str(iters), "--log-freq", str(10 * iters), "--out-dir",
+                            os.path.join(d, "out")], cwd=cwd, capture_output=True, text=True, timeout=1800)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference CLI failed on {png}: {r.stdout[-1000:]} {r.stderr[-1000:]}")
+        ref_psnr.append(float(re.findall(r"Final PSNR: ([0-9.]+)", r.stdout)[-1]))
+    ref_wall = time.perf_counter() - t0
+    cfg = train_config(log_freq=0, iterations=iters)
+    ours = {}
+    for w in (workers, 1):
+        with Executor(workers=w) as ex:
+            ex.submit_fit(imgs[0], config=train_config(log_freq=0, iterations=20)).result()
+            t0 = time.perf_counter()
+            reqs = [ex.submit_fit(img, config=cfg) for img in imgs]
+            ex.wait_all()
+            ours[w] = (time.perf_counter() - t0, [r.result()[1] for r in reqs])
+    mean = lambda xs: round(float(np.mean(xs)), 3)  # noqa: E731
+    return {"workload": f"batch of {count} images (bench.py --workload batch sizes), {iters} iterations, 1.0 bpp",
+            "images": [f"{i.shape[1]}x{i.shape[0]}" for i in imgs],
+            "reference_cli_sequential_wall_s": round(ref_wall, 3), "reference_psnr_mean": mean(ref_psnr),
+            "ours_executor_wall_s": round(ours[workers][0], 3), "ours_executor_workers": workers,
+            "ours_sequential_wall_s": round(ours[1][0], 3), "ours_psnr_mean": mean(ours[workers][1]),
+            "speedup_vs_reference": round(ref_wall / ours[workers][0], 2)}
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--batch", type=int, default=0, help="time the batch workload on this many images")
+    ap.add_argument("--iters", type=int, default=2000)
+    ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--repeats", type=int, default=2)
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--log-freq", type=int, default=1000)
     ap.add_argument("--seeds", type=int, default=1, help="images: synthetic seeds 0..N-1")
     args = ap.parse_args()
+    if args.batch:
+        print(json.dumps(run_batch(args.batch, args.iters, args.workers)))
+        return
     from sad_gb300 import imageio
     from sad_gb300.synthetic import quantize_u8, synthetic_image
     per_seed = []

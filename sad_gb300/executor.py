@@ -6,7 +6,8 @@
         sites, psnr = f.result()
         rgb = r.result()
 
-Each request keeps its host arrays alive until it completes.  Results are bitwise those
+The executor holds every request (and so the host arrays its worker reads and writes)
+until the request completes, whether or not the caller keeps it.  Results are bitwise those
 of a single fit (sad_trainer_fit_host) or render (sad_render_from_sites) of the same input.
 """
 from __future__ import annotations
@@ -36,6 +37,7 @@ class _Request:
         if not self._done:
             self._ex._check(self._ex._lib.sad_executor_wait(self._ex._h, self.ticket))
             self._done = True
+            self._ex._pending.pop(self.ticket.value, None)
         if self.res.status != 0:
             raise RequestError(self.res.message.decode(errors="replace"))
         return self
@@ -63,6 +65,7 @@ class Executor:
         cfg.workers = workers
         cfg.hbm_budget_bytes = hbm_budget_bytes
         self._h = C.c_void_p()
+        self._pending: dict[int, _Request] = {}  # submitted, not yet waited for
         self._check(self._lib.sad_executor_create(C.byref(cfg), C.byref(self._h)))
 
     def _check(self, status: int) -> None:
@@ -87,6 +90,7 @@ class Executor:
             self._h, C.byref(cfg), img.ctypes.data_as(C.c_void_p),
             None if m is None else m.ctypes.data_as(C.c_void_p), w, h,
             out.ctypes.data_as(C.c_void_p), cap, C.byref(req.res), C.byref(req.ticket)))
+        self._pending[req.ticket.value] = req
         return req
 
     def submit_render(self, sites: np.ndarray, width: int, height: int,
@@ -100,15 +104,25 @@ class Executor:
         self._check(self._lib.sad_executor_submit_render(
             self._h, C.byref(cfg), s.ctypes.data_as(C.c_void_p), s.shape[0], width, height,
             out.ctypes.data_as(C.c_void_p), C.byref(req.res), C.byref(req.ticket)))
+        self._pending[req.ticket.value] = req
         return req
 
     def wait_all(self) -> None:
         self._check(self._lib.sad_executor_wait_all(self._h))
+        for req in self._pending.values():
+            req._done = True
+        self._pending.clear()
 
     def close(self) -> None:
         if self._h:
-            self._lib.sad_executor_destroy(self._h)
+            self._lib.sad_executor_destroy(self._h)  # runs what is queued, then joins
             self._h = C.c_void_p()
+            for req in self._pending.values():
+                req._done = True
+            self._pending.clear()
+
+    def __del__(self):
+        self.close()
 
     def __enter__(self) -> "Executor":
         return self

@@ -120,3 +120,20 @@ def test_executor_argument_errors_and_drain(cuda):
     cfg.workers = 0
     h = C.c_void_p()
     assert lib.sad_executor_create(C.byref(cfg), C.byref(h)) != 0
+
+
+def test_executor_holds_unreferenced_requests(cuda):
+    """Requests whose handles the caller drops still own their host buffers until done."""
+    import gc
+    from sad_gb300.executor import Executor
+    img = cases.scene(64, 64, 8)[0]
+    ex = Executor(workers=2)
+    for _ in range(4):
+        ex.submit_fit(img, config=small_cfg(iterations=20))
+    ex.submit_render(cases.scene(64, 64, 9)[1], 64, 64)
+    gc.collect()
+    ex.wait_all()
+    kept = ex.submit_fit(img, config=small_cfg(iterations=20))
+    gc.collect()
+    ex.close()
+    assert kept.res.status == 0 and kept.result()[1] > 0
