@@ -431,6 +431,15 @@ size_t sad_render_scratch_bytes(uint32_t site_count, int width, int height, int 
 sad_status_t sad_render_from_sites(const sad_render_config_t* cfg, const float* sites,
                                    uint32_t site_count, int width, int height, float* out_rgb,
                                    void* scratch, size_t scratch_bytes, sad_stream_t stream);
+/* As sad_render_from_sites, then waits for it and reports the device time of the
+ * candidate build (JFA rounds and VPT passes, after the per-site preparation and the
+ * Hilbert order, as the reference times it) and of the render (CUDA events on the
+ * stream): the two numbers of the reference's "Candidate build: X ms | Render: Y ms"
+ * line (sad_cuda.cu:1760-1836). */
+sad_status_t sad_render_from_sites_timed(const sad_render_config_t* cfg, const float* sites,
+                                         uint32_t site_count, int width, int height, float* out_rgb,
+                                         void* scratch, size_t scratch_bytes, sad_stream_t stream,
+                                         float* cand_ms, float* render_ms);
 
 /* ------------------------------------------------------------------------ */
 /* 16-byte quantised inference sites (the Metal backend's serving format)     */

@@ -4,6 +4,7 @@ the identical 8-bit image (equal-PSNR speed comparison).  Prints one JSON line.
     oracle/ref/stage.sh /path/to/reference && oracle/ref/build.sh
     python oracle/ref/time_reference.py [--repeats 2] [--size 1024] [--seeds 4]
     python oracle/ref/time_reference.py --batch 64 [--iters 2000] [--workers 8]
+    python oracle/ref/time_reference.py --cli-compare --size 256 --sites 4096 --iters 200
 
 The reference binary (oracle/_ref/sad_cuda, built from the staged copy of its sources)
 reads training_config.json from its working directory (baseline/_ref/sad holds the staged
@@ -122,8 +123,81 @@ def run_batch(count: int, iters: int, workers: int):
             "speedup_vs_reference": round(ref_wall / ours[workers][0], 2)}
 
 
+def run_cli_compare(size: int, sites: int, iters: int, repeats: int, seeds: int = 1):
+    """Both command-line binaries with the same arguments on the same 8-bit image: a fit with
+    a fixed site count (densify, prune and the bpp rule off), then render-only from the
+    reference fit's sites file.  Best of `repeats` per binary."""
+    from sad_gb300 import imageio
+    from sad_gb300.synthetic import quantize_u8, synthetic_image
+    d = tempfile.mkdtemp()
+    pngs = []
+    for sd in range(seeds):
+        pngs.append(os.path.join(d, f"synthetic_{size}_s{sd}.png"))
+        imageio.save_image(pngs[-1], quantize_u8(synthetic_image(size, size, seed=sd)))
+    png = pngs[0]
+    staged = os.path.join(ROOT, "baseline", "_ref", "sad")
+    bins = {"reference": (os.path.join(ROOT, "oracle", "_ref", "sad_cuda"), dict(os.environ)),
+            "ours": (os.path.join(ROOT, "sad_gb300", "_lib", "sad_cuda"),
+                     dict(os.environ, CONFIG_PATH=os.path.join(staged, "training_config.json")))}
+    fit_args = ["--sites", str(sites), "--iters", str(iters), "--target-bpp", "0", "--densify-percentile", "0",
+                "--prune-percentile", "0", "--log-freq", str(10 * iters)]
+    out = {"workload": f"{size}x{size} synthetic (8-bit), {sites} sites fixed (densify, prune, bpp rule off), "
+                       f"{iters} iterations; then render-only from the reference fit's sites"}
+
+    def run(exe, env, args):
+        r = subprocess.run([exe, *args], cwd=staged, env=env, capture_output=True, text=True, timeout=1800)
+        if r.returncode != 0:
+            raise RuntimeError(f"{exe} failed: {r.stdout[-1500:]} {r.stderr[-1500:]}")
+        return r.stdout
+
+    for impl in ("reference", "ours"):
+        exe, env = bins[impl]
+        best = None
+        for k in range(repeats):
+            od = os.path.join(d, f"{impl}_{k}")
+            log = run(exe, env, [png, *fit_args, "--out-dir", od])
+            res = {"training_time_s": float(re.findall(r"Training time: ([0-9.]+) s", log)[-1]),
+                   "psnr_db": float(re.findall(r"Final PSNR: ([0-9.]+)", log)[-1]),
+                   "it_per_s_log": float(re.findall(r"\|\s*([0-9.]+) it/s", log)[-1])}
+            if best is None or res["training_time_s"] < best["training_time_s"]:
+                best = res
+        out[impl] = best
+    # PSNR over all seeds (one fit each) and the PSNR trajectory of the first image
+    for impl in ("reference", "ours"):
+        exe, env = bins[impl]
+        finals = []
+        for sd, p in enumerate(pngs):
+            log = run(exe, env, [p, *fit_args[:-1], str(20), "--out-dir", os.path.join(d, f"{impl}_seed{sd}")])
+            finals.append(float(re.findall(r"Final PSNR: ([0-9.]+)", log)[-1]))
+            if sd == 0:
+                out[impl]["psnr_trajectory"] = [(int(i), float(v)) for i, v in
+                                                re.findall(r"Iter +(\d+) \| PSNR: ([0-9.]+)", log)]
+        out[impl]["psnr_per_seed"] = finals
+        out[impl]["psnr_mean"] = round(float(np.mean(finals)), 3)
+    ref_sites = os.path.join(d, "reference_0", os.path.basename(png)[:-4] + "_sites.txt")
+    for impl in ("reference", "ours"):
+        exe, env = bins[impl]
+        best = None
+        for k in range(repeats):
+            log = run(exe, env, ["--render", ref_sites, "--render-target", png, "--out",
+                                 os.path.join(d, f"render_{impl}_{k}.png")])
+            m = re.findall(r"Candidate build: ([0-9.]+) ms \| Render: ([0-9.]+) ms", log)[-1]
+            res = {"cand_ms": float(m[0]), "render_ms": float(m[1]),
+                   "render_psnr_db": float(re.findall(r"Render PSNR: ([0-9.]+)", log)[-1])}
+            if best is None or res["cand_ms"] + res["render_ms"] < best["cand_ms"] + best["render_ms"]:
+                best = res
+        out[impl]["render_only"] = best
+    out["speedup_training"] = round(out["reference"]["training_time_s"] / out["ours"]["training_time_s"], 2)
+    ref_r, our_r = out["reference"]["render_only"], out["ours"]["render_only"]
+    out["speedup_render_only"] = round((ref_r["cand_ms"] + ref_r["render_ms"]) / (our_r["cand_ms"] + our_r["render_ms"]), 2)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--cli-compare", action="store_true",
+                    help="both CLIs, fixed-site fit + render-only (--size, --sites, --iters)")
+    ap.add_argument("--sites", type=int, default=4096)
     ap.add_argument("--batch", type=int, default=0, help="time the batch workload on this many images")
     ap.add_argument("--iters", type=int, default=2000)
     ap.add_argument("--workers", type=int, default=8)
@@ -134,6 +208,9 @@ def main():
     args = ap.parse_args()
     if args.batch:
         print(json.dumps(run_batch(args.batch, args.iters, args.workers)))
+        return
+    if args.cli_compare:
+        print(json.dumps(run_cli_compare(args.size, args.sites, args.iters, args.repeats, args.seeds)))
         return
     from sad_gb300 import imageio
     from sad_gb300.synthetic import quantize_u8, synthetic_image

@@ -12,8 +12,7 @@ __version__ = "1.0.0"
 
 
 def _lazy_torch():
-    from . import modules, ops, torch_ops  # noqa: F401
-    torch_ops.register()
+    from . import modules, ops  # noqa: F401  (importing ops registers torch.ops.sad)
     return modules
 
 

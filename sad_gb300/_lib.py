@@ -127,6 +127,8 @@ SIGNATURES = {
     "sad_render_config_default": (None, [C.POINTER(RenderConfig)]),
     "sad_render_scratch_bytes": (sz, [u32, i32, i32, i32]),
     "sad_render_from_sites": (st, [C.POINTER(RenderConfig), vp, u32, i32, i32, vp, vp, sz, vp]),
+    "sad_render_from_sites_timed": (st, [C.POINTER(RenderConfig), vp, u32, i32, i32, vp, vp, sz, vp,
+                                         C.POINTER(f32), C.POINTER(f32)]),
     "sad_pack_inference_sites": (st, [vp, u32, i32, i32, vp, vp, vp]),
     "sad_unpack_inference_sites": (st, [vp, vp, u32, i32, i32, vp, vp]),
     "sad_render_packed": (st, [vp, vp, vp, vp, vp, f32, u32, i32, i32, i32, i32, vp]),

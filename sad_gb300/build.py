@@ -88,6 +88,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
         run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs])
         os.replace(tmp, lib)
     build_cli(force=force, verbose=verbose)
+    build_torch_ops(force=force, verbose=verbose)
     return lib
 
 
@@ -115,6 +116,48 @@ def build_cli(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError(f"CLI build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(exe + ".tmp", exe)
     return exe
+
+
+TORCH_EXT_DIR = os.path.join(PKG, "torch_ext")
+
+
+def torch_ops_path() -> str:
+    return os.path.join(OUT_DIR, "libsad_torch_ops.so")
+
+
+def build_torch_ops(force: bool = False, verbose: bool = False) -> str | None:
+    """The torch.ops.sad operator library (host C++ against torch's headers, on the C ABI).
+    Skipped, returning None, when torch is not importable."""
+    try:
+        import torch
+        from torch.utils import cpp_extension as ce
+    except ImportError:
+        return None
+    src = os.path.join(TORCH_EXT_DIR, "sad_torch_ops.cpp")
+    out = torch_ops_path()
+    deps = [src, os.path.join(INCLUDE, "sad_gb300.h"), lib_path(), os.path.abspath(__file__), torch.__file__]
+    if not force and not _stale(out, deps):
+        return out
+    try:
+        incs = ce.include_paths(device_type="cuda")
+        libs = ce.library_paths(device_type="cuda")
+    except TypeError:  # older signature
+        incs = ce.include_paths(cuda=True)
+        libs = ce.library_paths(cuda=True)
+    cuda_home = os.path.dirname(os.path.dirname(nvcc()))
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-w",
+           f"-D_GLIBCXX_USE_CXX11_ABI={int(torch._C._GLIBCXX_USE_CXX11_ABI)}",
+           "-I" + INCLUDE, "-I" + os.path.join(cuda_home, "include"), *["-I" + i for i in incs],
+           src, "-o", out + ".tmp", "-L" + OUT_DIR, "-lsad_gb300", *["-L" + d for d in libs],
+           "-lc10", "-lc10_cuda", "-ltorch", "-ltorch_cpu", "-ltorch_cuda",
+           "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"torch operator build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(out + ".tmp", out)
+    return out
 
 
 if __name__ == "__main__":

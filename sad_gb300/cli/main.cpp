@@ -660,32 +660,23 @@ int render(Options& o) {
     const size_t npix = static_cast<size_t>(w) * h;
     DeviceBuf<float> d_sites(ls.sites.size()), d_out(npix * 3);
     check_cuda(cudaMemcpy(d_sites.p, ls.sites.data(), ls.sites.size() * 4, cudaMemcpyHostToDevice), "upload");
-    size_t scratch_bytes = o.render_packed ? sad_render_packed_scratch_bytes(n, w, h, o.rcfg.cand_downscale)
-                                           : sad_render_scratch_bytes(n, w, h, o.rcfg.cand_downscale);
+    size_t scratch_bytes = sad_render_scratch_bytes(n, w, h, o.rcfg.cand_downscale);
     DeviceBuf<unsigned char> d_scratch(scratch_bytes);
     DeviceBuf<uint32_t> d_packed(o.render_packed ? size_t(n) * 4 : 1);
     DeviceBuf<sad_packed_quant_t> d_quant(1);
     if (o.render_packed) {
+        // 16-byte sites: pack, then render what they decode to (the packed render path)
         if (w > 32768 || h > 32768) die("--render-packed: image side above 32768");
         check(sad_pack_inference_sites(d_sites.p, n, w, h, d_packed.p, d_quant.p, nullptr),
               "sad_pack_inference_sites");
+        check(sad_unpack_inference_sites(d_packed.p, d_quant.p, n, w, h, d_sites.p, nullptr),
+              "sad_unpack_inference_sites");
         std::printf("Packed inference sites: %u x 16 bytes\n", n);
     }
-    cudaEvent_t e0, e1;
-    check_cuda(cudaEventCreate(&e0), "event");
-    check_cuda(cudaEventCreate(&e1), "event");
-    check_cuda(cudaEventRecord(e0, nullptr), "event");
-    if (o.render_packed)
-        check(sad_render_packed_from_sites(&o.rcfg, d_packed.p, d_quant.p, n, w, h, d_out.p, d_scratch.p,
-                                           scratch_bytes, nullptr),
-              "sad_render_packed_from_sites");
-    else
-        check(sad_render_from_sites(&o.rcfg, d_sites.p, n, w, h, d_out.p, d_scratch.p, scratch_bytes, nullptr),
-              "sad_render_from_sites");
-    check_cuda(cudaEventRecord(e1, nullptr), "event");
-    check_cuda(cudaEventSynchronize(e1), "render");
-    float ms = 0.0f;
-    check_cuda(cudaEventElapsedTime(&ms, e0, e1), "event");
+    float cand_ms = 0.0f, render_ms = 0.0f;
+    check(sad_render_from_sites_timed(&o.rcfg, d_sites.p, n, w, h, d_out.p, d_scratch.p, scratch_bytes, nullptr,
+                                      &cand_ms, &render_ms),
+          "sad_render_from_sites");
     if (!o.render_target.empty()) {
         Image8 timg = load_png_or_die(o.render_target, "render target");
         if (timg.width != w || timg.height != h) {
@@ -701,8 +692,7 @@ int render(Options& o) {
             std::printf("Render PSNR: %.2f dB\n", psnr_of(sum, double(npix)));
         }
     }
-    // the candidate build (JFA + VPT passes) and the render run in one call
-    std::printf("Candidate build + render: %.3f ms\n", ms);
+    std::printf("Candidate build: %.3f ms | Render: %.3f ms\n", cand_ms, render_ms);
     std::vector<float> out(npix * 3);
     check_cuda(cudaMemcpy(out.data(), d_out.p, npix * 12, cudaMemcpyDeviceToHost), "download");
     std::string out_path = o.out_path.empty()
@@ -712,8 +702,6 @@ int render(Options& o) {
         std::printf("Saved: %s\n", out_path.c_str());
     else
         std::fprintf(stderr, "Failed to save: %s\n", out_path.c_str());
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     return 0;
 }
 

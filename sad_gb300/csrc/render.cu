@@ -192,10 +192,12 @@ void launch_clear_candidates(uint32_t* c0, uint32_t* c1, int w, int h, cudaStrea
 // ---------------------------------------------------------------------------
 // autograd adjoint (backends/pytorch/torch_ext/cuda/sad_bindings.cu:41-207)
 // ---------------------------------------------------------------------------
-constexpr int kBwdSlots = 512;
-
-template <class Src>
-__global__ void __launch_bounds__(256) render_backward_kernel(
+// Key-table size per 256-pixel tile: 256 slots while sites are sparse enough (at most one
+// per four pixels: a tile then sees well under 200 distinct candidates), 512 above that.
+// Four blocks per SM (64 registers a thread) keep 32 warps resident for the latency of the
+// shared-memory atomics.
+template <class Src, int kBwdSlots>
+__global__ void __launch_bounds__(256, 4) render_backward_kernel(
     const uint4* __restrict__ cand0, const uint4* __restrict__ cand1,
     const float* __restrict__ grad_rgb, float* __restrict__ grad_sites, Src src, float inv_s2,
     uint32_t n, int w, int h, int cw, int ch) {
@@ -304,10 +306,16 @@ __global__ void __launch_bounds__(256) render_backward_kernel(
 void launch_render_backward_raw(const uint32_t* c0, const uint32_t* c1, const float* grad_rgb,
                                 float* grad_sites, const Site* sites, float inv_s2, uint32_t n,
                                 int w, int h, int cw, int ch, cudaStream_t st) {
-    render_backward_kernel<RawSites><<<pixel_grid(w, h), dim3(32, 8),
-                                       sizeof(TileTable<10, kBwdSlots, AccFloat>), st>>>(
-        reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), grad_rgb,
-        grad_sites, RawSites{sites}, inv_s2, n, w, h, cw, ch);
+    auto c0v = reinterpret_cast<const uint4*>(c0);
+    auto c1v = reinterpret_cast<const uint4*>(c1);
+    if (static_cast<double>(n) * 4.0 <= static_cast<double>(w) * h)
+        render_backward_kernel<RawSites, 256><<<pixel_grid(w, h), dim3(32, 8),
+                                                sizeof(TileTable<10, 256, AccFloat>), st>>>(
+            c0v, c1v, grad_rgb, grad_sites, RawSites{sites}, inv_s2, n, w, h, cw, ch);
+    else
+        render_backward_kernel<RawSites, 512><<<pixel_grid(w, h), dim3(32, 8),
+                                                sizeof(TileTable<10, 512, AccFloat>), st>>>(
+            c0v, c1v, grad_rgb, grad_sites, RawSites{sites}, inv_s2, n, w, h, cw, ch);
     note_launches(1);
 }
 

@@ -66,11 +66,11 @@ extern "C" size_t sad_render_scratch_bytes(uint32_t site_count, int width, int h
     return carve(nullptr, site_count, cw, ch).total;
 }
 
-extern "C" sad_status_t sad_render_from_sites(const sad_render_config_t* cfg, const float* sites_f,
-                                              uint32_t n, int width, int height, float* out_rgb,
-                                              void* scratch, size_t scratch_bytes,
-                                              sad_stream_t stream) {
-    clear_error();
+// ev (nullable): three events recorded before the candidate build, before the render and
+// after it.
+static sad_status_t render_from_sites_impl(const sad_render_config_t* cfg, const float* sites_f, uint32_t n,
+                                           int width, int height, float* out_rgb, void* scratch,
+                                           size_t scratch_bytes, sad_stream_t stream, cudaEvent_t* ev) {
     SAD_REQUIRE(cfg, "sad_render_from_sites: null config");
     SAD_REQUIRE(width > 0 && height > 0, "sad_render_from_sites: invalid size");
     SAD_REQUIRE(n > 0 && sites_f && out_rgb && scratch, "sad_render_from_sites: null buffer or no sites");
@@ -106,6 +106,9 @@ extern "C" sad_status_t sad_render_from_sites(const sad_render_config_t* cfg, co
         launch_radix_sort(r.hpairs, padded, maxk, r.sort_temp, st);
         launch_hilbert_order(r.hpairs, r.horder, r.hpos, n, st);
     }
+    // the timed candidate build starts here, where the reference starts it: after the
+    // per-site preparation, the packed copy and the Hilbert order (sad_cuda.cu:1760-1786)
+    if (ev) SAD_TRY(check_cuda(cudaEventRecord(ev[0], st), "sad_render_from_sites: event"));
     uint32_t jump_pass = 0;
     for (int round = 0; round < rounds; ++round) {
         if (cfg->use_jfa) {
@@ -154,7 +157,38 @@ extern "C" sad_status_t sad_render_from_sites(const sad_render_config_t* cfg, co
             a = 1 - a;
         }
     }
+    if (ev) SAD_TRY(check_cuda(cudaEventRecord(ev[1], st), "sad_render_from_sites: event"));
     launch_render_prepared(r.c0[a], r.c1[a], out_rgb, r.geom, r.color, inv_s2, n, width, height, cw,
                            ch, st);
+    if (ev) SAD_TRY(check_cuda(cudaEventRecord(ev[2], st), "sad_render_from_sites: event"));
     return check_launch("sad_render_from_sites");
+}
+
+extern "C" sad_status_t sad_render_from_sites(const sad_render_config_t* cfg, const float* sites_f,
+                                              uint32_t n, int width, int height, float* out_rgb,
+                                              void* scratch, size_t scratch_bytes,
+                                              sad_stream_t stream) {
+    clear_error();
+    return render_from_sites_impl(cfg, sites_f, n, width, height, out_rgb, scratch, scratch_bytes, stream,
+                                  nullptr);
+}
+
+extern "C" sad_status_t sad_render_from_sites_timed(const sad_render_config_t* cfg, const float* sites_f,
+                                                    uint32_t n, int width, int height, float* out_rgb,
+                                                    void* scratch, size_t scratch_bytes, sad_stream_t stream,
+                                                    float* cand_ms, float* render_ms) {
+    clear_error();
+    SAD_REQUIRE(cand_ms && render_ms, "sad_render_from_sites_timed: null timing output");
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    sad_status_t s = SAD_OK;
+    for (auto& e : ev)
+        if (s == SAD_OK) s = check_cuda(cudaEventCreate(&e), "sad_render_from_sites_timed: event");
+    if (s == SAD_OK)
+        s = render_from_sites_impl(cfg, sites_f, n, width, height, out_rgb, scratch, scratch_bytes, stream, ev);
+    if (s == SAD_OK) s = check_cuda(cudaEventSynchronize(ev[2]), "sad_render_from_sites_timed: sync");
+    if (s == SAD_OK) s = check_cuda(cudaEventElapsedTime(cand_ms, ev[0], ev[1]), "sad_render_from_sites_timed");
+    if (s == SAD_OK) s = check_cuda(cudaEventElapsedTime(render_ms, ev[1], ev[2]), "sad_render_from_sites_timed");
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    return s;
 }

@@ -1,15 +1,17 @@
-"""Registers the reference's `torch.ops.sad` operator schemas, implemented by sad_gb300.ops.
+"""The reference's `torch.ops.sad` operators, registered from C++.
 
-The schema strings are those of backends/pytorch/torch_ext/torch_binding.cpp:6-30, so code
-written against the reference extension (`torch.ops.sad.render_sad(...)`) runs unchanged.
-If another library already defined the `sad` namespace (the reference extension itself),
-registration is skipped and `sad_gb300.ops` remains available directly.
+libsad_torch_ops.so (built from sad_gb300/torch_ext/sad_torch_ops.cpp by sad_gb300.build)
+defines the schemas of backends/pytorch/torch_ext/torch_binding.cpp:6-30 verbatim and
+implements every operator in C++ on libsad_gb300's C ABI, so code written against the
+reference extension (`torch.ops.sad.render_sad(...)`) runs unchanged, with the host cost of
+a C++ operator.  If another library already owns the `sad` namespace (the reference
+extension itself), registration is refused and `register()` returns False.
 """
 from __future__ import annotations
 
-import torch
+import os
 
-from . import ops
+import torch
 
 SCHEMAS = {
     "render_sad": "render_sad(Tensor cand0, Tensor cand1, Tensor sites, float inv_scale_sq, int width, int height) -> Tensor",
@@ -38,26 +40,26 @@ SCHEMAS = {
     "init_gradient_weighted": "init_gradient_weighted(Tensor sites, Tensor target, Tensor mask, int site_count, float init_log_tau, float init_radius, float gradient_alpha) -> Tensor",
 }
 
-_LIBRARY = None
+LIBRARY_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libsad_torch_ops.so")
 REGISTERED = False
 
 
 def register() -> bool:
-    """Define torch.ops.sad.* once per process; returns True if this module owns them."""
-    global _LIBRARY, REGISTERED
+    """Load the operator library once per process; True when these operators own
+    torch.ops.sad, False when another library registered the namespace first."""
+    global REGISTERED
     if REGISTERED:
         return True
+    if not os.path.exists(LIBRARY_PATH):
+        from . import build
+        build.build()
+    if not os.path.exists(LIBRARY_PATH):
+        raise RuntimeError(f"{LIBRARY_PATH} is missing (PyTorch was not importable at build time)")
     try:
-        lib = torch.library.Library("sad", "DEF")
-    except RuntimeError:
-        return False
-    for name, schema in SCHEMAS.items():
-        lib.define(schema)
-        impl = getattr(ops, name)
-        if name == "init_candidates":
-            lib.impl(name, impl, "CompositeExplicitAutograd")
-        else:
-            lib.impl(name, impl, "CUDA")
-    _LIBRARY = lib
+        torch.ops.load_library(LIBRARY_PATH)
+    except (RuntimeError, OSError) as e:
+        if "sad" in str(e) and ("TORCH_LIBRARY" in str(e) or "namespace" in str(e)):
+            return False
+        raise
     REGISTERED = True
     return True

@@ -67,7 +67,7 @@ def test_cli_fit_then_render(sad_cuda, image, tmp_path):
     assert f"Loaded {sites.shape[0]} sites" in log and "Render size: 96x80" in log
     psnr = float(re.search(r"Render PSNR: ([0-9.]+) dB", log).group(1))
     assert psnr > final - 1.0
-    assert re.search(r"Candidate build \+ render: [0-9.]+ ms", log)
+    assert re.search(r"Candidate build: [0-9.]+ ms \| Render: [0-9.]+ ms", log)
     back = imageio.read_png(str(tmp_path / "results" / "synth_sites_render.png"))
     assert back.shape == (80, 96, 3)
     # the training render and the re-render see the same sites: most pixels agree closely

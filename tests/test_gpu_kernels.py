@@ -76,11 +76,21 @@ def test_render_all_invalid_black(ops):
     assert torch.count_nonzero(out).item() == 0
 
 
-@pytest.mark.parametrize("w,h,n,seed", [(64, 48, 256, 5), (200, 130, 3000, 6)])
-def test_render_backward_matches_oracle(ops, orc, w, h, n, seed):
+# The last two cases are dense (more than one site per four pixels: the 512-slot tables):
+# a nearest-neighbour field, and a random field whose tiles see far more distinct sites
+# than the table holds (the global-atomic path), with log_tau 2 so that the softmax over
+# far-apart candidates stays well conditioned in FP32 (the FP32 oracle matches its FP64
+# form there; with log_tau 5 a few entries of such a field differ between the two).
+@pytest.mark.parametrize("w,h,n,seed,field,log_tau", [(64, 48, 256, 5, "random", None),
+                                                       (200, 130, 3000, 6, "random", None),
+                                                       (48, 40, 1920, 7, "knn", None),
+                                                       (48, 40, 1920, 7, "random", 2.0)])
+def test_render_backward_matches_oracle(ops, orc, w, h, n, seed, field, log_tau):
     img, sites = cases.scene(w, h, n, seed)
     sites[::11, 0] = -1.0
-    c0, c1 = cases.random_field(w, h, n, seed)
+    if log_tau is not None:
+        sites[:, 2] = log_tau
+    c0, c1 = cases.knn_field(sites, w, h) if field == "knn" else cases.random_field(w, h, n, seed)
     gout = np.random.default_rng(seed).normal(size=(h, w, 3)).astype(np.float32)
     got = ops.render_sad_backward(t32(c0), t32(c1), tf(sites), tf(gout), 1.0 / max(w, h) ** 2, w, h)
     want, absw = orc.render_backward(c0, c1, sites, gout, w, h)
