@@ -9,8 +9,11 @@ set -uo pipefail
 HERE=$(cd "$(dirname "$0")/../.." && pwd)
 SRC="$HERE/baseline/_ref/sad/src"
 TP="$HERE/baseline/_ref/sad/third_party"
-OUT="$HERE/oracle/_ref"
-ARCH="-gencode arch=compute_103a,code=sm_103a"
+# REF_OUT / REF_ARCH select another output folder under oracle/_ref and another target,
+# e.g. REF_ARCH="-gencode arch=compute_86,code=compute_86" for the reference's shipped
+# sm_86 PTX, compiled by the driver at load time.
+OUT="${REF_OUT:-$HERE/oracle/_ref}"
+ARCH="${REF_ARCH:--gencode arch=compute_103a,code=sm_103a}"
 mkdir -p "$OUT"
 KERNELS="render jfa candidate_pack gradients adam tau_diffusion densify_prune radix_sort utils"
 pids=()

@@ -30,8 +30,11 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path[:0] = [ROOT]
 
 
+REF_EXE = os.path.join(ROOT, "oracle", "_ref", "sad_cuda")
+
+
 def run_reference(png: str, repeats: int, log_freq: int):
-    exe = os.path.join(ROOT, "oracle", "_ref", "sad_cuda")
+    exe = REF_EXE
     cwd = os.path.join(ROOT, "baseline", "_ref", "sad")
     best = None
     for _ in range(repeats):
@@ -88,7 +91,7 @@ def run_batch(count: int, iters: int, workers: int):
     from sad_gb300 import imageio
     from sad_gb300.config import train_config
     from sad_gb300.executor import Executor
-    exe = os.path.join(ROOT, "oracle", "_ref", "sad_cuda")
+    exe = REF_EXE
     cwd = os.path.join(ROOT, "baseline", "_ref", "sad")
     imgs = bench.batch_images(count)
     d = tempfile.mkdtemp()
@@ -136,7 +139,7 @@ def run_cli_compare(size: int, sites: int, iters: int, repeats: int, seeds: int 
         imageio.save_image(pngs[-1], quantize_u8(synthetic_image(size, size, seed=sd)))
     png = pngs[0]
     staged = os.path.join(ROOT, "baseline", "_ref", "sad")
-    bins = {"reference": (os.path.join(ROOT, "oracle", "_ref", "sad_cuda"), dict(os.environ)),
+    bins = {"reference": (REF_EXE, dict(os.environ)),
             "ours": (os.path.join(ROOT, "sad_gb300", "_lib", "sad_cuda"),
                      dict(os.environ, CONFIG_PATH=os.path.join(staged, "training_config.json")))}
     fit_args = ["--sites", str(sites), "--iters", str(iters), "--target-bpp", "0", "--densify-percentile", "0",
@@ -205,7 +208,12 @@ def main():
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--log-freq", type=int, default=1000)
     ap.add_argument("--seeds", type=int, default=1, help="images: synthetic seeds 0..N-1")
+    ap.add_argument("--ref-exe", default=None, help="reference CLI binary (default oracle/_ref/sad_cuda)")
+    ap.add_argument("--reference-only", action="store_true", help="time only the reference CLI")
     args = ap.parse_args()
+    global REF_EXE
+    if args.ref_exe:
+        REF_EXE = os.path.abspath(args.ref_exe)
     if args.batch:
         print(json.dumps(run_batch(args.batch, args.iters, args.workers)))
         return
@@ -220,11 +228,19 @@ def main():
         png = os.path.join(tempfile.mkdtemp(), f"synthetic_{args.size}_s{seed}.png")
         imageio.save_image(png, img)
         ref = run_reference(png, args.repeats, args.log_freq)
+        if args.reference_only:
+            per_seed.append({"seed": seed, "reference_cuda_cli": ref})
+            continue
         ours = run_ours(img, args.repeats)
         per_seed.append({"seed": seed, "reference_cuda_cli": ref, "ours": ours,
                          "speedup_it_per_s": round(ours["it_per_s"] / ref["it_per_s"], 2)
                          if ref.get("it_per_s") else None})
-    mean = lambda xs: round(float(np.mean(xs)), 3)
+    mean = lambda xs: round(float(np.mean(xs)), 3)  # noqa: E731
+    if args.reference_only:
+        print(json.dumps({"reference_exe": REF_EXE, "per_seed": per_seed,
+                          "reference_it_per_s_mean": mean([p["reference_cuda_cli"]["it_per_s"] for p in per_seed]),
+                          "reference_psnr_mean": mean([p["reference_cuda_cli"]["psnr_db"] for p in per_seed])}))
+        return
     out = {"workload": f"{args.size}x{args.size} synthetic (8-bit), training_config.json defaults",
            "seeds": args.seeds, "per_seed": per_seed,
            "reference_it_per_s_mean": mean([p["reference_cuda_cli"]["it_per_s"] for p in per_seed]),
