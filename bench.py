@@ -39,10 +39,9 @@ DATA = "synthetic: seeded smooth gradient + 256 Gaussian blobs + 64 convex polyg
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from sad_gb300.replicas import rank_env
+    e = rank_env()
+    return e.world_size, e.rank, e.local_rank
 
 
 class ClockSampler:
@@ -124,11 +123,11 @@ def flush_l2(buf):
 
 def run_ours(args):
     import torch
-    ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    from sad_gb300 import replicas
+    env = replicas.rank_env()
+    ws, rank, local = env.world_size, env.rank, env.local_rank
     torch.cuda.set_device(local)
+    replicas.init(env, "nccl")
     import sad_gb300
     from sad_gb300 import _lib
     from sad_gb300.synthetic import synthetic_image
@@ -156,8 +155,7 @@ def run_ours(args):
 
     for _ in range(args.warmup):
         one_fit(False)
-    if ws > 1:
-        torch.distributed.barrier()
+    replicas.barrier(env)
     torch.cuda.synchronize()
     launches0 = lib.sad_launch_count()
     times = []
@@ -166,11 +164,7 @@ def run_ours(args):
             times.append(one_fit(True))
     torch.cuda.synchronize()
     launches = lib.sad_launch_count() - launches0
-    total_ms = float(sum(times))
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replicas.max_over_ranks(env, float(sum(times)), device="cuda")
     psnr = tr.psnr()
     final_sites = tr.info().active_estimate
     value = ws * args.steps * iters / (total_ms / 1e3)
@@ -209,8 +203,7 @@ def run_ours(args):
            "d2h_bytes_per_step": int(tr.info().site_buffer * 40 + 4), "psnr_db": round(e2e_psnr, 3),
            "ms_per_fit": round(1e3 * float(np.mean(e2e_t)), 2)}
     tr.close()
-    if ws > 1:
-        torch.distributed.destroy_process_group()
+    replicas.finish(env)
     if rank != 0:
         return None
     out = {
