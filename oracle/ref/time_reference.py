@@ -190,6 +190,15 @@ def run_cli_compare(size: int, sites: int, iters: int, repeats: int, seeds: int 
             if best is None or res["cand_ms"] + res["render_ms"] < best["cand_ms"] + best["render_ms"]:
                 best = res
         out[impl]["render_only"] = best
+    # file-format interoperability: each CLI renders the other's sites file
+    ours_sites = os.path.join(d, "ours_0", os.path.basename(png)[:-4] + "_sites.txt")
+    cross = {}
+    for impl in ("reference", "ours"):
+        exe, env = bins[impl]
+        log = run(exe, env, ["--render", ours_sites, "--render-target", png, "--out",
+                             os.path.join(d, f"cross_{impl}.png")])
+        cross[f"ours_sites_rendered_by_{impl}_psnr_db"] = float(re.findall(r"Render PSNR: ([0-9.]+)", log)[-1])
+    out["cross_render"] = cross
     out["speedup_training"] = round(out["reference"]["training_time_s"] / out["ours"]["training_time_s"], 2)
     ref_r, our_r = out["reference"]["render_only"], out["ours"]["render_only"]
     out["speedup_render_only"] = round((ref_r["cand_ms"] + ref_r["render_ms"]) / (our_r["cand_ms"] + our_r["render_ms"]), 2)

@@ -144,3 +144,23 @@ def test_cli_packed_psnr_and_render_packed(sad_cuda, image, tmp_path):
     psnr = float(re.search(r"Render PSNR: ([0-9.]+) dB", log).group(1))
     assert psnr > packed - 1.0
     assert imageio.read_png(str(tmp_path / "packed_render.png")).shape == (80, 96, 3)
+
+
+def test_cli_renders_json_sites_like_txt(sad_cuda, image, tmp_path):
+    """The reference's JSON sites layout (sad_cuda.cu:340-389: image_width/image_height,
+    sites[] of pos, color, log_tau, radius, aniso_dir, log_aniso) renders exactly as the
+    same sites in TXT form."""
+    import json
+    out = tmp_path / "fit"
+    _fit(sad_cuda, image, out)
+    txt = out / "synth_sites.txt"
+    sites, w, h = sites_io.load_sites(str(txt))
+    doc = {"image_width": w, "image_height": h,
+           "sites": [{"pos": [float(s[0]), float(s[1])], "log_tau": float(s[2]), "radius": float(s[3]),
+                      "color": [float(s[4]), float(s[5]), float(s[6])], "aniso_dir": [float(s[7]), float(s[8])],
+                      "log_aniso": float(s[9])} for s in sites]}
+    js = tmp_path / "sites.json"
+    js.write_text(json.dumps(doc))
+    _run(sad_cuda, ["--render", str(txt), "--out", str(tmp_path / "a.png")], tmp_path)
+    _run(sad_cuda, ["--render", str(js), "--out", str(tmp_path / "b.png")], tmp_path)
+    np.testing.assert_array_equal(imageio.read_png(str(tmp_path / "a.png")), imageio.read_png(str(tmp_path / "b.png")))
