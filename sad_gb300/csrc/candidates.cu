@@ -258,7 +258,7 @@ __device__ __forceinline__ void vpt_pixel(const VptParams& prm, const Src& src, 
 }
 
 template <class Src>
-__global__ void __launch_bounds__(256) vpt_kernel(VptParams prm, Src src) {
+__global__ void __launch_bounds__(256, 5) vpt_kernel(VptParams prm, Src src) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= prm.width || y >= prm.height) return;
