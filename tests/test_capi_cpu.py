@@ -99,3 +99,16 @@ def test_torch_op_schemas_registered():
     for name in torch_ops.SCHEMAS:
         op = getattr(torch.ops.sad, name)
         assert str(op.default._schema).startswith("sad::" + name)
+
+
+def test_sad_ops_package_mirrors_the_reference_extension():
+    """`sad_ops` (the reference extension's package name) and the `sad_ops._sad_ext` module
+    its loader imports register this library's operators."""
+    import importlib
+
+    import torch
+    importlib.import_module("sad_ops._sad_ext")
+    import sad_ops
+    assert sad_ops.ops is torch.ops.sad
+    for name in ("render_sad", "render_sad_padded", "render_sad_backward", "init_candidates", "vpt_pass"):
+        assert getattr(sad_ops, name) is getattr(torch.ops.sad, name)
