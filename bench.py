@@ -401,16 +401,35 @@ def render_sites(side: int, seed: int):
 def run_serve(args):
     import torch
     from sad_gb300.config import train_config
-    from sad_gb300.executor import Executor
     from sad_gb300.synthetic import quantize_u8, synthetic_image
     torch.cuda.set_device(0)
     rates = [float(r) for r in args.serve_rates.split(",")]
     fit_cfg = train_config(log_freq=0, iterations=500)
     fit_imgs = {s: quantize_u8(synthetic_image(s, s, seed=s)) for s in (256, 320, 448, 576, 768, 1024)}
-    sites_cache = {}
     budget = int(args.serve_budget_gb * (1 << 30))
+    rows = serve_sweep(args, rates, args.workers, budget, fit_cfg, fit_imgs)
+    seq_rows = serve_sweep(args, rates, 1, budget, fit_cfg, fit_imgs) if args.serve_sequential else None
+    top = rows[-1]
+    return {
+        "metric": SERVE_METRIC, "value": top["p99_ms"], "unit": "ms", "n_gpus": 1, "steps": len(rates),
+        "warmup": 1, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: random 1-bpp site sets for renders, seeded synthetic images for fits",
+        "config": {"workload": f"{args.serve_count} requests per rate, Poisson arrivals at {rates} /s, "
+                               f"{args.workers} workers, HBM budget {args.serve_budget_gb} GB",
+                   "latency": "submission to results in host memory"},
+        "rates": rows,
+        "sequential_rates": seq_rows,
+        "e2e": {"value": top["p99_ms"], "unit": "ms", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+    }
+
+
+def serve_sweep(args, rates, workers, budget, fit_cfg, fit_imgs):
+    """The request streams of every rate through one executor of `workers` workers."""
+    from sad_gb300.config import train_config
+    from sad_gb300.executor import Executor
+    sites_cache = {}
     rows = []
-    with Executor(workers=args.workers, hbm_budget_bytes=budget) as ex:
+    with Executor(workers=workers, hbm_budget_bytes=budget) as ex:
         for kind, side, i in serve_requests(8, 99):  # warm-up
             if kind == "fit":
                 ex.submit_fit(fit_imgs[side], config=train_config(log_freq=0, iterations=50))
@@ -438,31 +457,26 @@ def run_serve(args):
             ex.wait_all()
             elapsed = time.perf_counter() - t0
             lat = {"fit": [], "render": []}
+            fit_psnr = []
             for k, r in zip(kinds, subs):
                 assert r.res.status == 0, r.res.message
                 lat[k].append(r.queue_ms + r.run_ms)
+                if k == "fit":
+                    fit_psnr.append(float(r.res.psnr))
             subs.clear()
             sites_cache.clear()
             allv = lat["fit"] + lat["render"]
             row = {"rate_per_s": rate, "requests": len(allv), "completed_per_s": round(len(allv) / elapsed, 2),
                    "p50_ms": round(float(np.percentile(allv, 50)), 1),
                    "p99_ms": round(float(np.percentile(allv, 99)), 1)}
+            if fit_psnr:
+                row["fit_psnr_mean_db"] = round(float(np.mean(fit_psnr)), 2)
             for k in ("render", "fit"):
                 if lat[k]:
                     row[f"{k}_p50_ms"] = round(float(np.percentile(lat[k], 50)), 1)
                     row[f"{k}_p99_ms"] = round(float(np.percentile(lat[k], 99)), 1)
             rows.append(row)
-    top = rows[-1]
-    return {
-        "metric": SERVE_METRIC, "value": top["p99_ms"], "unit": "ms", "n_gpus": 1, "steps": len(rates),
-        "warmup": 1, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic: random 1-bpp site sets for renders, seeded synthetic images for fits",
-        "config": {"workload": f"{args.serve_count} requests per rate, Poisson arrivals at {rates} /s, "
-                               f"{args.workers} workers, HBM budget {args.serve_budget_gb} GB",
-                   "latency": "submission to results in host memory"},
-        "rates": rows,
-        "e2e": {"value": top["p99_ms"], "unit": "ms", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
-    }
+    return rows
 
 
 def run_profile(args):
@@ -502,6 +516,8 @@ def main():
     ap.add_argument("--serve-rates", default="5,10,20,40")
     ap.add_argument("--serve-count", type=int, default=60)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-sequential", action="store_true",
+                    help="also run the same request streams with one worker (requests one at a time)")
     args = ap.parse_args()
     if args.mode == "profile":
         run_profile(args)
