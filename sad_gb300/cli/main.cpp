@@ -79,9 +79,16 @@ Defaults load_defaults() {
         die(std::string("training_config.json: ") + e.what());
     }
     sad_train_config_t& c = d.train;
-    auto seti = [&](const char* k, int& v) { if (j.has(k)) v = static_cast<int>(j.at(k).number()); };
-    auto setu = [&](const char* k, uint32_t& v) { if (j.has(k)) v = static_cast<uint32_t>(j.at(k).number()); };
-    auto setf = [&](const char* k, float& v) { if (j.has(k)) v = static_cast<float>(j.at(k).number()); };
+    auto num = [&](const char* k) -> double {
+        try {
+            return j.at(k).number();
+        } catch (const std::exception& e) {
+            die(std::string("training_config.json: ") + k + ": " + e.what());
+        }
+    };
+    auto seti = [&](const char* k, int& v) { if (j.has(k)) v = static_cast<int>(num(k)); };
+    auto setu = [&](const char* k, uint32_t& v) { if (j.has(k)) v = static_cast<uint32_t>(num(k)); };
+    auto setf = [&](const char* k, float& v) { if (j.has(k)) v = static_cast<float>(num(k)); };
     seti("DEFAULT_SITES", c.n_sites);
     seti("DEFAULT_MAX_SITES", c.max_sites);
     seti("DEFAULT_ITERS", c.iterations);

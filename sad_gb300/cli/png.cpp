@@ -254,6 +254,8 @@ Image8 read_png(const std::string& path) {
         pos += 12 + size_t(len);
     }
     if (w == 0 || h == 0 || ctype < 0) throw std::runtime_error("PNG without IHDR");
+    if (w > (1u << 24) || h > (1u << 24) || uint64_t(w) * h > (uint64_t(1) << 31))
+        throw std::runtime_error("PNG dimensions too large");
     if (interlace) throw std::runtime_error("interlaced PNG is not supported");
     int chans = ctype == 0 ? 1 : ctype == 2 ? 3 : ctype == 3 ? 1 : ctype == 4 ? 2 : ctype == 6 ? 4 : 0;
     if (!chans) throw std::runtime_error("unsupported PNG colour type");

@@ -109,9 +109,13 @@ sad_status_t run_render(const Request& q, void* mem, cudaStream_t ws) {
 }
 
 void worker_main(sad_executor* ex) {
-    if (cudaSetDevice(ex->device) != cudaSuccess) return;
+    // a worker whose device or stream cannot be set up still takes requests and fails
+    // each with that error, so no waiter is left behind
     cudaStream_t ws = nullptr;
-    if (cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking) != cudaSuccess) return;
+    sad_status_t setup = sad::check_cuda(cudaSetDevice(ex->device), "executor worker: device");
+    if (setup == SAD_OK)
+        setup = sad::check_cuda(cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking), "executor worker: stream");
+    const std::string setup_error = setup == SAD_OK ? std::string() : std::string(sad_last_error());
     for (;;) {
         Request q;
         {
@@ -132,7 +136,9 @@ void worker_main(sad_executor* ex) {
         r->queue_ms = std::chrono::duration<double, std::milli>(start - q.submitted).count();
         sad::clear_error();
         void* mem = nullptr;
-        sad_status_t st = sad::check_cuda(cudaMallocAsync(&mem, q.need, ws), "executor: slab allocation");
+        sad_status_t st = setup;
+        if (st != SAD_OK) sad::set_error("%s", setup_error.c_str());
+        if (st == SAD_OK) st = sad::check_cuda(cudaMallocAsync(&mem, q.need, ws), "executor: slab allocation");
         if (st == SAD_OK) st = sad::check_cuda(cudaStreamSynchronize(ws), "executor: slab allocation");
         if (st == SAD_OK) st = q.kind == 0 ? run_fit(q, mem, r) : run_render(q, mem, ws);
         set_message(r, st);
@@ -149,7 +155,7 @@ void worker_main(sad_executor* ex) {
         ex->cv_done.notify_all();
         ex->cv_work.notify_all();
     }
-    cudaStreamDestroy(ws);
+    if (ws) cudaStreamDestroy(ws);
 }
 
 sad_status_t enqueue(sad_executor_t* ex, Request&& q, uint64_t* ticket) {

@@ -173,6 +173,8 @@ def test_png_decoder_rejects_bad_files(png_check, tmp_path):
         "truncated": good[: len(good) // 2],
         "interlaced": good.replace(struct.pack(">IIBBBBB", 8, 8, 8, 2, 0, 0, 0),
                                    struct.pack(">IIBBBBB", 8, 8, 8, 2, 0, 0, 1)),
+        "huge": good.replace(struct.pack(">IIBBBBB", 8, 8, 8, 2, 0, 0, 0),
+                             struct.pack(">IIBBBBB", 1 << 20, 1 << 20, 8, 2, 0, 0, 0)),
     }
     for name, data in bad.items():
         p = tmp_path / f"{name}.png"
@@ -223,6 +225,11 @@ def test_cli_configuration_errors(sad_cuda, tmp_path):
     r = _run(sad_cuda, ["x.png"], tmp_path, p)
     assert r.returncode == 1
     assert "INIT_LOG_TAU and INIT_RADIUS must be set" in r.stderr
+    cfg = json.load(open(PACKAGED_CONFIG))
+    cfg["PRUNE_FREQ"] = "forty"
+    p.write_text(json.dumps(cfg))
+    r = _run(sad_cuda, ["--help"], tmp_path, p)
+    assert r.returncode == 1 and "PRUNE_FREQ" in r.stderr
 
 
 @pytest.mark.parametrize("args,needle", [
