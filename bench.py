@@ -108,13 +108,13 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """Per-launch DRAM bytes of the fused gradient kernel from the committed ncu summary."""
+def profiled_kernel():
+    """The fused gradient kernel's committed ncu summary (DRAM bytes per launch, limiter)."""
     try:
         with open(os.path.join(ROOT, "profiles", "fused_gradients_1024.json")) as f:
-            return json.load(f).get("dram_bytes_per_launch")
+            return json.load(f)
     except (OSError, ValueError):
-        return None
+        return {}
 
 
 def flush_l2(buf):
@@ -184,7 +184,8 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (grad_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(),
+                "frac": round(achieved / peak, 4), "traffic": profiled_kernel().get("dram_bytes_per_launch"),
+                "limiter": profiled_kernel().get("limiter"),
                 "kernel": "fused_gradients_kernel", "launch_ms": round(grad_ms, 5),
                 "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
 
