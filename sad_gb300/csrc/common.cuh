@@ -17,6 +17,8 @@
 //   * SiteColor (16 B): r, g, b, pad.
 #pragma once
 
+#include <utility>
+
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -52,6 +54,29 @@ struct DevState {
     float adam_c1;      // Adam bias corrections 1 / (1 - beta^t) for t = iter + 1
     float adam_c2;
 };
+
+// Programmatic dependent launch: a kernel launched with the programmatic-serialization
+// attribute may start while the previous kernel in its stream drains; it waits here, before
+// reading anything that kernel wrote, for that kernel's completion and memory.  A no-op for a
+// normally launched kernel.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Launch with programmatic stream serialization (the kernel must call pdl_wait() first).
+template <class... KArgs, class... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 __device__ __forceinline__ int clampi(int x, int a, int b) { return max(a, min(b, x)); }
 __device__ __forceinline__ float clampf(float x, float a, float b) { return fmaxf(a, fminf(b, x)); }

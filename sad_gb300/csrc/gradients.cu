@@ -341,6 +341,7 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
 // rotated register arrays.
 template <class Src, bool kRemoval, bool kSSIM>
 __global__ void __launch_bounds__(256, 4) fused_gradients_pre_kernel(GradParams prm, Src src) {
+    pdl_wait();
     using L = GradLayout<true, kRemoval>;
     constexpr int NV = L::NV;
     auto& sm = shared_table<typename L::Pre>();
@@ -505,8 +506,8 @@ static void launch_fused(const GradParams& p, Src src, cudaStream_t st) {
     dim3 grid((p.width + 15) / 16, (p.height + 15) / 16);
     if constexpr (kFix) {
         if (p.slot_map) {
-            fused_gradients_pre_kernel<Src, kRemoval, kSSIM>
-                <<<grid, 256, sizeof(typename GradLayout<true, kRemoval>::Pre), st>>>(p, src);
+            launch_pdl(fused_gradients_pre_kernel<Src, kRemoval, kSSIM>, grid, dim3(256),
+                       sizeof(typename GradLayout<true, kRemoval>::Pre), st, p, src);
             return;
         }
     }

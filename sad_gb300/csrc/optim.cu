@@ -94,6 +94,7 @@ __global__ void tau_first_pass_kernel(const uint4* __restrict__ c0, const uint4*
                                       float* __restrict__ gout, uint32_t n,
                                       const DevState* __restrict__ state, int iterations, int w,
                                       int h, int ds) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float2 sp = __ldg(reinterpret_cast<const float2*>(geom + i));
@@ -157,6 +158,7 @@ __device__ __forceinline__ float tau_list_pass(const TauLists& tl, const float* 
 __global__ void tau_list_pass_kernel(TauLists tl, const float* __restrict__ gin,
                                      float* __restrict__ gout, uint32_t n,
                                      const DevState* __restrict__ state, int iterations) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !tl.active[i]) return;
     gout[i] = tau_list_pass(tl, gin, i, tau_lambda(state->iter, iterations));
@@ -168,9 +170,9 @@ void launch_tau_first_pass(const uint32_t* c0, const uint32_t* c1, const SiteGeo
                            int h, int ds, cudaStream_t st) {
     if (n == 0) return;
     TauLists tl{reinterpret_cast<uint4*>(nbr), raw, active};
-    tau_first_pass_kernel<<<blocks_for(n, 256), 256, 0, st>>>(
-        reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), geom, fix12, tl,
-        gout, n, state, iterations, w, h, ds);
+    launch_pdl(tau_first_pass_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st,
+               reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), geom, fix12, tl, gout, n,
+               state, iterations, w, h, ds);
     note_launches(1);
 }
 
@@ -180,7 +182,7 @@ void launch_tau_list_pass(const uint32_t* nbr, const float* raw, const uint8_t* 
     if (n == 0) return;
     TauLists tl{reinterpret_cast<uint4*>(const_cast<uint32_t*>(nbr)), const_cast<float*>(raw),
                 const_cast<uint8_t*>(active)};
-    tau_list_pass_kernel<<<blocks_for(n, 256), 256, 0, st>>>(tl, gin, gout, n, state, iterations);
+    launch_pdl(tau_list_pass_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st, tl, gin, gout, n, state, iterations);
     note_launches(1);
 }
 
@@ -340,6 +342,7 @@ __global__ void adam_train_kernel(Site* __restrict__ sites, float* __restrict__ 
                                   SiteColor* __restrict__ color, AdamHyper hp,
                                   const DevState* __restrict__ state, int iterations, uint32_t n,
                                   int w, int h) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !tl.active[i]) return;
     const float tau_g = tau_list_pass(tl, tau_gin, i, tau_lambda(state->iter, iterations));
@@ -373,8 +376,8 @@ void launch_adam_train(Site* sites, float* adam, long long* fix12, const uint32_
     if (n == 0) return;
     TauLists tl{reinterpret_cast<uint4*>(const_cast<uint32_t*>(nbr)), const_cast<float*>(raw),
                 const_cast<uint8_t*>(active)};
-    adam_train_kernel<<<blocks_for(n, 256), 256, 0, st>>>(sites, adam, fix12, tl, tau_gin, geom,
-                                                          color, hp, state, iterations, n, w, h);
+    launch_pdl(adam_train_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st, sites, adam, fix12, tl, tau_gin,
+               geom, color, hp, state, iterations, n, w, h);
     note_launches(1);
 }
 
@@ -414,6 +417,7 @@ __global__ void reset_state_kernel(DevState* state, float beta1, float beta2) {
 }
 
 __global__ void advance_state_kernel(DevState* state, uint32_t vpt_passes, float beta1, float beta2) {
+    pdl_wait();
     state->iter += 1u;
     state->vpt_pass += vpt_passes;
     set_bias_corrections(state, beta1, beta2);
@@ -426,7 +430,7 @@ void launch_reset_state(DevState* state, float beta1, float beta2, cudaStream_t 
 
 void launch_advance_state(DevState* state, uint32_t vpt_passes, float beta1, float beta2,
                           cudaStream_t st) {
-    advance_state_kernel<<<1, 1, 0, st>>>(state, vpt_passes, beta1, beta2);
+    launch_pdl(advance_state_kernel, dim3(1), dim3(1), 0, st, state, vpt_passes, beta1, beta2);
     note_launches(1);
 }
 
