@@ -259,6 +259,7 @@ __device__ __forceinline__ void vpt_pixel(const VptParams& prm, const Src& src, 
 
 template <class Src>
 __global__ void __launch_bounds__(256, 5) vpt_kernel(VptParams prm, Src src) {
+    pdl_wait();
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= prm.width || y >= prm.height) return;
@@ -269,13 +270,13 @@ __global__ void __launch_bounds__(256, 5) vpt_kernel(VptParams prm, Src src) {
 static dim3 pixel_grid(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }
 
 void launch_vpt_packed(const VptParams& prm, const uint16_t* packed, cudaStream_t st) {
-    vpt_kernel<PackedHalfSites><<<pixel_grid(prm.width, prm.height), dim3(32, 8), 0, st>>>(
+    launch_pdl(vpt_kernel<PackedHalfSites>, pixel_grid(prm.width, prm.height), dim3(32, 8), 0, st,
         prm, PackedHalfSites{reinterpret_cast<const uint4*>(packed)});
     note_launches(1);
 }
 
 void launch_vpt_geom(const VptParams& prm, const SiteGeom* geom, cudaStream_t st) {
-    vpt_kernel<PackedGeomSites><<<pixel_grid(prm.width, prm.height), dim3(32, 8), 0, st>>>(
+    launch_pdl(vpt_kernel<PackedGeomSites>, pixel_grid(prm.width, prm.height), dim3(32, 8), 0, st,
         prm, PackedGeomSites{geom});
     note_launches(1);
 }
@@ -348,6 +349,7 @@ __global__ void __launch_bounds__(256) jfa_flood_kernel(const uint4* __restrict_
                                                         uint4* __restrict__ out0, Src src,
                                                         uint32_t n, uint32_t step, float inv_s2,
                                                         int w, int h, int ds, int tw, int th) {
+    pdl_wait();
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
@@ -375,7 +377,7 @@ __global__ void __launch_bounds__(256) jfa_flood_kernel(const uint4* __restrict_
 void launch_jfa_flood_raw(const uint32_t* in0, uint32_t* out0, const Site* sites, uint32_t n,
                           uint32_t step, float inv_s2, int w, int h, int ds, int tw, int th,
                           cudaStream_t st) {
-    jfa_flood_kernel<RawGeomSites><<<pixel_grid(w, h), dim3(32, 8), 0, st>>>(
+    launch_pdl(jfa_flood_kernel<RawGeomSites>, pixel_grid(w, h), dim3(32, 8), 0, st,
         reinterpret_cast<const uint4*>(in0), reinterpret_cast<uint4*>(out0), RawGeomSites{sites},
         n, step, inv_s2, w, h, ds, tw, th);
     note_launches(1);
@@ -384,7 +386,7 @@ void launch_jfa_flood_raw(const uint32_t* in0, uint32_t* out0, const Site* sites
 void launch_jfa_flood_geom(const uint32_t* in0, uint32_t* out0, const SiteGeom* geom, uint32_t n,
                            uint32_t step, float inv_s2, int w, int h, int ds, int tw, int th,
                            cudaStream_t st) {
-    jfa_flood_kernel<FullGeomSites><<<pixel_grid(w, h), dim3(32, 8), 0, st>>>(
+    launch_pdl(jfa_flood_kernel<FullGeomSites>, pixel_grid(w, h), dim3(32, 8), 0, st,
         reinterpret_cast<const uint4*>(in0), reinterpret_cast<uint4*>(out0), FullGeomSites{geom},
         n, step, inv_s2, w, h, ds, tw, th);
     note_launches(1);

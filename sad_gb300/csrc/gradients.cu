@@ -455,6 +455,7 @@ __global__ void __launch_bounds__(256, 4) fused_gradients_pre_kernel(GradParams 
 __global__ void __launch_bounds__(256) register_tiles_kernel(const uint4* __restrict__ c0,
                                                              const uint4* __restrict__ c1, uint32_t n,
                                                              int w, int h, int cw, int ch, TileMap map) {
+    pdl_wait();
     __shared__ KeyTable<512> table;
     const int tid = threadIdx.x;
     table.init_keys(tid, 256);
@@ -495,9 +496,8 @@ TileMap tile_map_at(uint32_t* base, int w, int h) {
 void launch_register_tiles(const uint32_t* c0, const uint32_t* c1, uint32_t n, int w, int h,
                            int cw, int ch, const TileMap& map, cudaStream_t st) {
     dim3 grid((w + 15) / 16, (h + 15) / 16);
-    register_tiles_kernel<<<grid, 256, 0, st>>>(reinterpret_cast<const uint4*>(c0),
-                                                  reinterpret_cast<const uint4*>(c1), n, w, h, cw, ch,
-                                                  map);
+    launch_pdl(register_tiles_kernel, grid, dim3(256), 0, st, reinterpret_cast<const uint4*>(c0),
+               reinterpret_cast<const uint4*>(c1), n, w, h, cw, ch, map);
     note_launches(1);
 }
 

@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(256) render_kernel(const uint4* __restrict__ c
                                                      int cw, int ch) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
+    pdl_wait();
     if (x >= w || y >= h) return;
     src.prepare();
     int p = y * w + x;
@@ -108,9 +109,9 @@ void launch_render_raw(const uint32_t* c0, const uint32_t* c1, float* out, const
 void launch_render_prepared(const uint32_t* c0, const uint32_t* c1, float* out,
                             const SiteGeom* geom, const SiteColor* color, float inv_s2,
                             uint32_t n, int w, int h, int cw, int ch, cudaStream_t st) {
-    render_kernel<PreparedSites><<<pixel_grid(w, h), dim3(32, 8), 0, st>>>(
-        reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), out,
-        PreparedSites{geom, color}, inv_s2, n, w, h, cw, ch);
+    launch_pdl(render_kernel<PreparedSites>, pixel_grid(w, h), dim3(32, 8), 0, st,
+               reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), out,
+               PreparedSites{geom, color}, inv_s2, n, w, h, cw, ch);
     note_launches(1);
 }
 
