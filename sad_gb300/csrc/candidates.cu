@@ -64,6 +64,7 @@ __device__ __forceinline__ SiteGeom geom_from_packed(uint4 v) {
 // pass instead of 16-byte gathers plus two expf and a division per visit).
 __global__ void pack_geom_kernel(const Site* __restrict__ sites, SiteGeom* __restrict__ out,
                                  uint32_t n) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float2* q = reinterpret_cast<const float2*>(sites + i);
@@ -89,7 +90,7 @@ __global__ void pack_geom_kernel(const Site* __restrict__ sites, SiteGeom* __res
 
 void launch_pack_geom(const Site* sites, SiteGeom* out, uint32_t n, cudaStream_t st) {
     if (n == 0) return;
-    pack_geom_kernel<<<blocks_for(n, 256), 256, 0, st>>>(sites, out, n);
+    launch_pdl(pack_geom_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st, sites, out, n);
     note_launches(1);
 }
 
@@ -294,6 +295,7 @@ __device__ __forceinline__ int seed_texel(float px, float py, int w, int h, int 
 // Two phases give a deterministic winner (the lowest id) where sites share a texel.
 __global__ void jfa_seed_mark_kernel(uint32_t* __restrict__ cand0, const Site* __restrict__ sites,
                                      uint32_t n, int w, int h, int ds) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float px = sites[i].px;
@@ -303,6 +305,7 @@ __global__ void jfa_seed_mark_kernel(uint32_t* __restrict__ cand0, const Site* _
 
 __global__ void jfa_seed_min_kernel(uint32_t* __restrict__ cand0, const Site* __restrict__ sites,
                                     uint32_t n, int w, int h, int ds) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float px = sites[i].px;
@@ -313,8 +316,8 @@ __global__ void jfa_seed_min_kernel(uint32_t* __restrict__ cand0, const Site* __
 void launch_jfa_seed(uint32_t* cand0, const Site* sites, uint32_t n, int w, int h, int ds,
                      cudaStream_t st) {
     if (n == 0) return;
-    jfa_seed_mark_kernel<<<blocks_for(n, 256), 256, 0, st>>>(cand0, sites, n, w, h, ds);
-    jfa_seed_min_kernel<<<blocks_for(n, 256), 256, 0, st>>>(cand0, sites, n, w, h, ds);
+    launch_pdl(jfa_seed_mark_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st, cand0, sites, n, w, h, ds);
+    launch_pdl(jfa_seed_min_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st, cand0, sites, n, w, h, ds);
     note_launches(2);
 }
 

@@ -16,6 +16,7 @@ namespace sad {
 // ---------------------------------------------------------------------------
 __global__ void prepare_sites_kernel(const Site* __restrict__ sites, SiteGeom* __restrict__ geom,
                                      SiteColor* __restrict__ color, uint32_t n) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float2* q = reinterpret_cast<const float2*>(sites + i);
@@ -27,7 +28,7 @@ __global__ void prepare_sites_kernel(const Site* __restrict__ sites, SiteGeom* _
 void launch_prepare_sites(const Site* sites, SiteGeom* geom, SiteColor* color, uint32_t n,
                           cudaStream_t st) {
     if (n == 0) return;
-    prepare_sites_kernel<<<blocks_for(n, 256), 256, 0, st>>>(sites, geom, color, n);
+    launch_pdl(prepare_sites_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st, sites, geom, color, n);
     note_launches(1);
 }
 
@@ -136,6 +137,7 @@ void launch_render_packed(const uint32_t* c0, const uint32_t* c1, float* out, co
 // ---------------------------------------------------------------------------
 __global__ void init_candidates_kernel(uint4* __restrict__ c0, uint4* __restrict__ c1, uint32_t n,
                                        uint32_t seed, int per_pixel, int w, int h) {
+    pdl_wait();
     int x = blockIdx.x * blockDim.x + threadIdx.x;
     int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
@@ -166,6 +168,7 @@ __global__ void init_candidates_kernel(uint4* __restrict__ c0, uint4* __restrict
 
 __global__ void fill_u32x4_kernel(uint4* __restrict__ a, uint4* __restrict__ b, size_t count,
                                   uint32_t v) {
+    pdl_wait();
     size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
     size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
     uint4 f = make_uint4(v, v, v, v);
@@ -177,16 +180,16 @@ __global__ void fill_u32x4_kernel(uint4* __restrict__ a, uint4* __restrict__ b, 
 
 void launch_init_candidates(uint32_t* c0, uint32_t* c1, uint32_t n, uint32_t seed, int per_pixel,
                             int w, int h, cudaStream_t st) {
-    init_candidates_kernel<<<pixel_grid(w, h), dim3(32, 8), 0, st>>>(
-        reinterpret_cast<uint4*>(c0), reinterpret_cast<uint4*>(c1), n, seed, per_pixel, w, h);
+    launch_pdl(init_candidates_kernel, pixel_grid(w, h), dim3(32, 8), 0, st, reinterpret_cast<uint4*>(c0),
+               reinterpret_cast<uint4*>(c1), n, seed, per_pixel, w, h);
     note_launches(1);
 }
 
 void launch_clear_candidates(uint32_t* c0, uint32_t* c1, int w, int h, cudaStream_t st) {
     size_t count = static_cast<size_t>(w) * h;
     unsigned blocks = static_cast<unsigned>(std::min<size_t>((count + 255) / 256, 152 * 16));
-    fill_u32x4_kernel<<<blocks, 256, 0, st>>>(reinterpret_cast<uint4*>(c0),
-                                               reinterpret_cast<uint4*>(c1), count, kEmpty);
+    launch_pdl(fill_u32x4_kernel, dim3(blocks), dim3(256), 0, st, reinterpret_cast<uint4*>(c0),
+               reinterpret_cast<uint4*>(c1), count, kEmpty);
     note_launches(1);
 }
 

@@ -36,6 +36,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_hist_kernel(const uint2* __
                                                                  uint32_t* __restrict__ hist,
                                                                  uint32_t count, uint32_t shift,
                                                                  uint32_t tiles) {
+    pdl_wait();
     __shared__ uint32_t bins[256];
     int tid = threadIdx.x;
     bins[tid] = 0;
@@ -58,6 +59,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_hist_kernel(const uint2* __
 __global__ void __launch_bounds__(1024) scan_single_kernel(uint32_t* __restrict__ data,
                                                            uint32_t count,
                                                            uint32_t* __restrict__ total) {
+    pdl_wait();
     __shared__ uint32_t warp_sums[32];
     int tid = threadIdx.x;
     uint32_t per = (count + 1023) / 1024;
@@ -98,6 +100,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_scatter_kernel(const uint2*
                                                                     const uint32_t* __restrict__ offs,
                                                                     uint32_t count, uint32_t shift,
                                                                     uint32_t tiles) {
+    pdl_wait();
     __shared__ uint32_t base[256];
     __shared__ uint32_t warp_cnt[kSortThreads / 32][256];
     int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -134,7 +137,7 @@ __global__ void __launch_bounds__(kSortThreads) sort_scatter_kernel(const uint2*
 }
 
 void launch_scan_single(uint32_t* data, uint32_t count, uint32_t* total, cudaStream_t st) {
-    scan_single_kernel<<<1, 1024, 0, st>>>(data, count, total);
+    launch_pdl(scan_single_kernel, dim3(1), dim3(1024), 0, st, data, count, total);
     note_launches(1);
 }
 
@@ -151,9 +154,9 @@ void launch_radix_sort(uint32_t* pairs, uint32_t count, uint32_t max_key_exclusi
     uint2* b = scratch;
     for (int pass = 0; pass < passes; ++pass) {
         uint32_t shift = static_cast<uint32_t>(pass) * 8u;
-        sort_hist_kernel<<<tiles, kSortThreads, 0, st>>>(a, hist, count, shift, tiles);
-        scan_single_kernel<<<1, 1024, 0, st>>>(hist, 256u * tiles, nullptr);
-        sort_scatter_kernel<<<tiles, kSortThreads, 0, st>>>(a, b, hist, count, shift, tiles);
+        launch_pdl(sort_hist_kernel, dim3(tiles), dim3(kSortThreads), 0, st, a, hist, count, shift, tiles);
+        launch_pdl(scan_single_kernel, dim3(1), dim3(1024), 0, st, hist, 256u * tiles, nullptr);
+        launch_pdl(sort_scatter_kernel, dim3(tiles), dim3(kSortThreads), 0, st, a, b, hist, count, shift, tiles);
         uint2* tmp = a;
         a = b;
         b = tmp;

@@ -507,6 +507,7 @@ __host__ __device__ inline uint32_t hilbert_index(uint32_t x, uint32_t y, int bi
 
 __global__ void hilbert_pairs_kernel(const Site* __restrict__ sites, uint2* __restrict__ pairs,
                                      uint32_t n, uint32_t padded, int w, int h, int bits) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= padded) return;
     if (i < n) {
@@ -522,13 +523,14 @@ __global__ void hilbert_pairs_kernel(const Site* __restrict__ sites, uint2* __re
 void launch_hilbert_pairs(const Site* sites, uint32_t* pairs, uint32_t n, uint32_t padded, int w,
                           int h, int bits, cudaStream_t st) {
     if (padded == 0) return;
-    hilbert_pairs_kernel<<<blocks_for(padded, 256), 256, 0, st>>>(
-        sites, reinterpret_cast<uint2*>(pairs), n, padded, w, h, bits);
+    launch_pdl(hilbert_pairs_kernel, dim3(blocks_for(padded, 256)), dim3(256), 0, st, sites,
+               reinterpret_cast<uint2*>(pairs), n, padded, w, h, bits);
     note_launches(1);
 }
 
 __global__ void hilbert_order_kernel(const uint2* __restrict__ pairs, uint32_t* __restrict__ order,
                                      uint32_t* __restrict__ pos, uint32_t n) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t s = pairs[i].y;
@@ -539,8 +541,8 @@ __global__ void hilbert_order_kernel(const uint2* __restrict__ pairs, uint32_t* 
 void launch_hilbert_order(const uint32_t* pairs, uint32_t* order, uint32_t* pos, uint32_t n,
                           cudaStream_t st) {
     if (n == 0) return;
-    hilbert_order_kernel<<<blocks_for(n, 256), 256, 0, st>>>(reinterpret_cast<const uint2*>(pairs),
-                                                             order, pos, n);
+    launch_pdl(hilbert_order_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st,
+               reinterpret_cast<const uint2*>(pairs), order, pos, n);
     note_launches(1);
 }
 
