@@ -113,10 +113,11 @@ def run_batch(count: int, iters: int, workers: int):
     for w in (workers, 1):
         with Executor(workers=w) as ex:
             ex.submit_fit(imgs[0], config=train_config(log_freq=0, iterations=20)).result()
+            order = sorted(range(len(imgs)), key=lambda i: -imgs[i].shape[0] * imgs[i].shape[1])
             t0 = time.perf_counter()
-            reqs = [ex.submit_fit(img, config=cfg) for img in imgs]
+            sub = {i: ex.submit_fit(imgs[i], config=cfg) for i in order}  # largest first
             ex.wait_all()
-            ours[w] = (time.perf_counter() - t0, [r.result()[1] for r in reqs])
+            ours[w] = (time.perf_counter() - t0, [sub[i].result()[1] for i in range(len(imgs))])
     mean = lambda xs: round(float(np.mean(xs)), 3)  # noqa: E731
     return {"workload": f"batch of {count} images (bench.py --workload batch sizes), {iters} iterations, 1.0 bpp",
             "images": [f"{i.shape[1]}x{i.shape[0]}" for i in imgs],
