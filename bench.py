@@ -413,15 +413,16 @@ def run_serve(args):
     fit_cfg = train_config(log_freq=0, iterations=500)
     fit_imgs = {s: quantize_u8(synthetic_image(s, s, seed=s)) for s in (256, 320, 448, 576, 768, 1024)}
     budget = int(args.serve_budget_gb * (1 << 30))
-    rows = serve_sweep(args, rates, args.workers, budget, fit_cfg, fit_imgs)
-    seq_rows = serve_sweep(args, rates, 1, budget, fit_cfg, fit_imgs) if args.serve_sequential else None
+    rows = serve_sweep(args, rates, args.workers, budget, fit_cfg, fit_imgs, args.serve_max_fits)
+    seq_rows = serve_sweep(args, rates, 1, budget, fit_cfg, fit_imgs, 0) if args.serve_sequential else None
     top = rows[-1]
     return {
         "metric": SERVE_METRIC, "value": top["p99_ms"], "unit": "ms", "n_gpus": 1, "steps": len(rates),
         "warmup": 1, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic: random 1-bpp site sets for renders, seeded synthetic images for fits",
         "config": {"workload": f"{args.serve_count} requests per rate, Poisson arrivals at {rates} /s, "
-                               f"{args.workers} workers, HBM budget {args.serve_budget_gb} GB",
+                               f"{args.workers} workers, at most {args.serve_max_fits or 'any'} fits at once, "
+                               f"HBM budget {args.serve_budget_gb} GB",
                    "latency": "submission to results in host memory"},
         "rates": rows,
         "sequential_rates": seq_rows,
@@ -429,13 +430,13 @@ def run_serve(args):
     }
 
 
-def serve_sweep(args, rates, workers, budget, fit_cfg, fit_imgs):
+def serve_sweep(args, rates, workers, budget, fit_cfg, fit_imgs, max_fits):
     """The request streams of every rate through one executor of `workers` workers."""
     from sad_gb300.config import train_config
     from sad_gb300.executor import Executor
     sites_cache = {}
     rows = []
-    with Executor(workers=workers, hbm_budget_bytes=budget) as ex:
+    with Executor(workers=workers, hbm_budget_bytes=budget, max_running_fits=max_fits) as ex:
         for kind, side, i in serve_requests(8, 99):  # warm-up
             if kind == "fit":
                 ex.submit_fit(fit_imgs[side], config=train_config(log_freq=0, iterations=50))
@@ -520,8 +521,10 @@ def main():
     ap.add_argument("--batch-iters", type=int, default=2000)
     ap.add_argument("--batch-sequential", action="store_true", help="also time the batch with one worker")
     ap.add_argument("--serve-rates", default="5,10,20,40")
-    ap.add_argument("--serve-count", type=int, default=60)
+    ap.add_argument("--serve-count", type=int, default=120)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-max-fits", type=int, default=2,
+                    help="at most this many fits run at once in the serving executor (0: no cap)")
     ap.add_argument("--serve-sequential", action="store_true",
                     help="also run the same request streams with one worker (requests one at a time)")
     args = ap.parse_args()

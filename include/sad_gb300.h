@@ -500,7 +500,8 @@ sad_status_t sad_trainer_render_packed(sad_trainer_t* t, float* rgb_out, float* 
 /* executor: many fits and renders in flight on one GPU                       */
 /* ------------------------------------------------------------------------ */
 
-/* Host worker threads, each with its own streams, take requests first in, first out.
+/* Host worker threads, each with its own streams, take requests first in, first out
+ * (a render may pass a fit that waits for a fit slot).
  * Every request runs in one slab from the device's stream-ordered memory pool; a request
  * waits while the slabs of running requests plus its own exceed hbm_budget_bytes
  * (0: no limit; a request larger than the budget runs alone).
@@ -509,6 +510,8 @@ sad_status_t sad_trainer_render_packed(sad_trainer_t* t, float* rgb_out, float* 
 typedef struct {
     int workers;              /* default 8 */
     size_t hbm_budget_bytes;  /* default 0 */
+    int max_running_fits;     /* default 0 (no cap): at most this many fits run at once;
+                                 renders queued behind a waiting fit pass it */
 } sad_executor_config_t;
 
 typedef struct {

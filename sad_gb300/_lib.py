@@ -57,7 +57,7 @@ class RenderConfig(C.Structure):
 
 
 class ExecutorConfig(C.Structure):
-    _fields_ = [("workers", i32), ("hbm_budget_bytes", C.c_size_t)]
+    _fields_ = [("workers", i32), ("hbm_budget_bytes", C.c_size_t), ("max_running_fits", i32)]
 
 
 class RequestResult(C.Structure):

@@ -68,6 +68,8 @@ struct sad_executor {
     int device = 0;
     size_t budget = 0;  // 0: no limit
     size_t in_use = 0;
+    int max_fits = 0;   // 0: no limit
+    int running_fits = 0;
     bool stop = false;
     uint64_t next_ticket = 1;
     std::deque<Request> queue;
@@ -120,16 +122,24 @@ void worker_main(sad_executor* ex) {
         Request q;
         {
             std::unique_lock<std::mutex> lock(ex->mu);
-            auto admissible = [&] {
-                if (ex->queue.empty()) return false;
-                size_t need = ex->queue.front().need;
-                return ex->budget == 0 || ex->in_use == 0 || ex->in_use + need <= ex->budget;
+            // the earliest queued request that fits the memory budget and, for a fit, the
+            // cap on running fits (so renders pass fits that wait for a fit slot)
+            auto pick = [&]() -> std::deque<Request>::iterator {
+                for (auto it = ex->queue.begin(); it != ex->queue.end(); ++it) {
+                    bool mem = ex->budget == 0 || ex->in_use == 0 || ex->in_use + it->need <= ex->budget;
+                    bool slot = it->kind != 0 || ex->max_fits == 0 || ex->running_fits < ex->max_fits;
+                    if (mem && slot) return it;
+                    if (!mem) break;  // keep first-in-first-out order under memory pressure
+                }
+                return ex->queue.end();
             };
-            ex->cv_work.wait(lock, [&] { return admissible() || (ex->stop && ex->queue.empty()); });
+            ex->cv_work.wait(lock, [&] { return pick() != ex->queue.end() || (ex->stop && ex->queue.empty()); });
             if (ex->queue.empty()) break;  // stopped and drained
-            q = ex->queue.front();
-            ex->queue.pop_front();
+            auto it = pick();
+            q = *it;
+            ex->queue.erase(it);
             ex->in_use += q.need;
+            if (q.kind == 0) ++ex->running_fits;
         }
         sad_request_result_t* r = q.result;
         Clock::time_point start = Clock::now();
@@ -150,6 +160,7 @@ void worker_main(sad_executor* ex) {
         {
             std::lock_guard<std::mutex> lock(ex->mu);
             ex->in_use -= q.need;
+            if (q.kind == 0) --ex->running_fits;
             ex->inflight.erase(q.ticket);
         }
         ex->cv_done.notify_all();
@@ -178,6 +189,7 @@ extern "C" void sad_executor_config_default(sad_executor_config_t* cfg) {
     if (!cfg) return;
     cfg->workers = 8;
     cfg->hbm_budget_bytes = 0;
+    cfg->max_running_fits = 0;
 }
 
 extern "C" sad_status_t sad_executor_create(const sad_executor_config_t* cfg, sad_executor_t** out) {
@@ -187,6 +199,7 @@ extern "C" sad_status_t sad_executor_create(const sad_executor_config_t* cfg, sa
     *out = nullptr;
     auto* ex = new sad_executor();
     ex->budget = cfg->hbm_budget_bytes;
+    ex->max_fits = cfg->max_running_fits > 0 ? cfg->max_running_fits : 0;
     sad_status_t st = sad::check_cuda(cudaGetDevice(&ex->device), "sad_executor_create: device");
     if (st == SAD_OK) {
         // keep freed slabs in the pool between requests instead of returning them to the

@@ -58,12 +58,13 @@ class _Request:
 
 
 class Executor:
-    def __init__(self, workers: int = 8, hbm_budget_bytes: int = 0):
+    def __init__(self, workers: int = 8, hbm_budget_bytes: int = 0, max_running_fits: int = 0):
         self._lib = _lib.load()
         cfg = _lib.ExecutorConfig()
         self._lib.sad_executor_config_default(C.byref(cfg))
         cfg.workers = workers
         cfg.hbm_budget_bytes = hbm_budget_bytes
+        cfg.max_running_fits = max_running_fits
         self._h = C.c_void_p()
         self._pending: dict[int, _Request] = {}  # submitted, not yet waited for
         self._check(self._lib.sad_executor_create(C.byref(cfg), C.byref(self._h)))

@@ -116,7 +116,7 @@ def test_executor_argument_errors_and_drain(cuda):
     lib = _lib.load()
     cfg = _lib.ExecutorConfig()
     lib.sad_executor_config_default(C.byref(cfg))
-    assert cfg.workers == 8 and cfg.hbm_budget_bytes == 0
+    assert cfg.workers == 8 and cfg.hbm_budget_bytes == 0 and cfg.max_running_fits == 0
     cfg.workers = 0
     h = C.c_void_p()
     assert lib.sad_executor_create(C.byref(cfg), C.byref(h)) != 0
@@ -137,3 +137,33 @@ def test_executor_holds_unreferenced_requests(cuda):
     gc.collect()
     ex.close()
     assert kept.res.status == 0 and kept.result()[1] > 0
+
+
+def test_executor_fit_cap_lets_renders_pass(cuda):
+    """max_running_fits=1: fits run one at a time (their run intervals do not overlap) while
+    renders queued behind a waiting fit still start; results stay those of solo runs."""
+    import time
+    from sad_gb300.executor import Executor
+    imgs = [cases.scene(96, 80, 60 + i)[0] for i in range(3)]
+    cfg = small_cfg(iterations=120)
+    _, sites = cases.scene(128, 96, 70)
+    with Executor(workers=4, max_running_fits=1) as ex:
+        t0 = time.perf_counter()
+        fits = [ex.submit_fit(img, config=cfg) for img in imgs]
+        renders = [ex.submit_render(sites, 128, 96) for _ in range(3)]
+        ex.wait_all()
+        span = 1e3 * (time.perf_counter() - t0)
+        iv = sorted((r.queue_ms, r.queue_ms + r.run_ms) for r in fits)
+        for (a0, a1), (b0, b1) in zip(iv, iv[1:]):
+            assert b0 >= a1 - 0.5, iv  # submission times differ by well under 0.5 ms
+        # the renders did not wait for all three fits
+        assert min(r.queue_ms for r in renders) < iv[-1][0]
+        assert max(b for _, b in iv) <= span + 1.0
+        for req, img in zip(fits, imgs):
+            sites_out, psnr = req.result()
+            want, want_psnr = solo_fit(img, cfg)
+            assert psnr == want_psnr
+            np.testing.assert_array_equal(sites_out, want)
+        want_r = solo_render(sites, 128, 96)
+        for r in renders:
+            np.testing.assert_array_equal(r.result(), want_r)
