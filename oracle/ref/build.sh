@@ -11,7 +11,7 @@ SRC="$HERE/baseline/_ref/sad/src"
 TP="$HERE/baseline/_ref/sad/third_party"
 # REF_OUT / REF_ARCH select another output folder under oracle/_ref and another target,
 # e.g. REF_ARCH="-gencode arch=compute_86,code=compute_86" for the reference's shipped
-# sm_86 PTX, compiled by the driver at load time.
+# sm_86 PTX, compiled by the CUDA driver when the program loads.
 OUT="${REF_OUT:-$HERE/oracle/_ref}"
 ARCH="${REF_ARCH:--gencode arch=compute_103a,code=sm_103a}"
 mkdir -p "$OUT"

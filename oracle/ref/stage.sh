@@ -1,8 +1,9 @@
 #!/usr/bin/env bash
 # Copy the reference's CUDA backend sources (kernels, host driver, vendored IO headers,
-# training_config.json) and its PyTorch extension's CUDA bindings from the read-only reference checkout into baseline/_ref/, the
-# git-ignored location for the reference that travels with the repository snapshot to the
-# GPU machine.  Nothing here is committed; oracle/ref/build.sh compiles from that copy.
+# training_config.json) and its PyTorch extension's CUDA bindings from the read-only
+# reference checkout into baseline/_ref/, the git-ignored location of the reference that is
+# copied with the working tree to the machine with the GPU.  Nothing here is committed;
+# oracle/ref/build.sh compiles from that copy.
 #   usage: oracle/ref/stage.sh [/path/to/reference]
 set -euo pipefail
 REF=${1:-/root/reference}

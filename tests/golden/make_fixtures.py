@@ -1,7 +1,7 @@
 """Generate golden fixtures from the reference's own CUDA kernels.
 
     oracle/ref/stage.sh /path/to/reference     # copy its sources to baseline/_ref/ (git-ignored)
-    oracle/ref/build.sh                        # nvcc -> oracle/_ref/ref_harness (needs a GPU machine to run)
+    oracle/ref/build.sh                        # nvcc -> oracle/_ref/ref_harness (needs a GPU to run)
     python tests/golden/make_fixtures.py [outdir]
 
 Each case writes seeded inputs to a scratch directory, runs one reference kernel through
