@@ -131,9 +131,9 @@ Defaults load_defaults() {
 // ---------------------------------------------------------------------------
 // images (sad_cuda.cu:137-229)
 // ---------------------------------------------------------------------------
-Image8 load_png_or_die(const std::string& path, const char* what) {
+Image8 load_image_or_die(const std::string& path, const char* what) {
     try {
-        return sadcli::read_png(path);
+        return sadcli::read_image(path);
     } catch (const std::exception& e) {
         die(std::string("Failed to load ") + what + ": " + path + " (" + e.what() + ")");
     }
@@ -172,7 +172,7 @@ std::vector<float> to_float_rgb(const Image8& img) {
 // Mask: one channel in [0, 1] (grey files directly; colour files through an integer
 // luma, (77 r + 150 g + 29 b) >> 8), resampled to the target size.
 std::vector<float> load_mask(const std::string& path, int w, int h) {
-    Image8 m = load_png_or_die(path, "mask");
+    Image8 m = load_image_or_die(path, "mask");
     if (m.width != w || m.height != h) m = resample(m, w, h);
     std::vector<float> out(static_cast<size_t>(w) * h);
     for (size_t i = 0; i < out.size(); ++i) {
@@ -495,7 +495,7 @@ float psnr_of(float mse_sum, double npix) {
 // ---------------------------------------------------------------------------
 int train(Options& o) {
     const auto t_start = std::chrono::steady_clock::now();
-    Image8 img = load_png_or_die(o.image, "image");
+    Image8 img = load_image_or_die(o.image, "image");
     if (o.max_dim > 0 && std::max(img.width, img.height) > o.max_dim) {
         double s = double(o.max_dim) / std::max(img.width, img.height);
         img = resample(img, std::max(1, int(std::lround(img.width * s))), std::max(1, int(std::lround(img.height * s))));
@@ -685,7 +685,7 @@ int render(Options& o) {
                                       &cand_ms, &render_ms),
           "sad_render_from_sites");
     if (!o.render_target.empty()) {
-        Image8 timg = load_png_or_die(o.render_target, "render target");
+        Image8 timg = load_image_or_die(o.render_target, "render target");
         if (timg.width != w || timg.height != h) {
             std::fprintf(stderr, "Render target size mismatch; skipping PSNR.\n");
         } else {

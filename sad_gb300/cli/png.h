@@ -1,4 +1,5 @@
-// png.h -- PNG reading (8-bit RGB out) and writing (8-bit RGB) for the command-line host.
+// png.h -- image files for the command-line host: PNG reading (8-bit RGB out) and writing,
+// baseline JPEG reading (jpeg.cpp).
 #pragma once
 
 #include <cstdint>
@@ -16,5 +17,9 @@ struct Image8 {
 // Throws std::runtime_error on unreadable or unsupported files.
 Image8 read_png(const std::string& path);
 bool write_png(const std::string& path, const uint8_t* rgb, int width, int height);
+Image8 read_jpeg(const std::string& path);
+bool is_jpeg_file(const std::string& path);
+// PNG or JPEG by the file's leading bytes (the reference host reads both through one loader).
+Image8 read_image(const std::string& path);
 
 }  // namespace sadcli

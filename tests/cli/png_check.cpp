@@ -16,7 +16,7 @@ int main(int argc, char** argv) {
     try {
         std::string mode = argc > 1 ? argv[1] : "";
         if (mode == "read" && argc == 4) {
-            sadcli::Image8 img = sadcli::read_png(argv[2]);
+            sadcli::Image8 img = sadcli::read_image(argv[2]);
             std::FILE* f = std::fopen(argv[3], "wb");
             if (!f) return 1;
             std::fprintf(f, "%d %d %d\n", img.width, img.height, img.gray ? 1 : 0);

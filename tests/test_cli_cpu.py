@@ -1,6 +1,8 @@
 """The sad_cuda-compatible command-line host without a GPU: its PNG codec (sad_gb300/cli/png.cpp,
 driven through tests/cli/png_check.cpp) against PNGs encoded here with zlib over every colour
-type, bit depth and scanline filter the decoder accepts, and the argument / configuration
+type, bit depth and scanline filter the decoder accepts; its baseline JPEG reader
+(sad_gb300/cli/jpeg.cpp; the reference host reads JPEG through stb_image,
+backends/cuda/src/sad_cuda.cu:141) against files from tests/jpeg_encode.py; and the argument / configuration
 handling whose exit codes follow backends/cuda/src/sad_cuda.cu:459-517 (missing
 training_config.json or INIT_* keys -> exit 1) and :754-895 (--help -> 0, unknown flag -> 1).
 """
@@ -99,8 +101,8 @@ def png_check(tmp_path_factory):
     if cxx is None:
         pytest.skip("no host C++ compiler")
     exe = str(tmp_path_factory.mktemp("png") / "png_check")
-    subprocess.run([cxx, "-O1", "-std=c++17", "-I" + CLI_SRC, os.path.join(ROOT, "tests", "cli", "png_check.cpp"),
-                    os.path.join(CLI_SRC, "png.cpp"), "-o", exe], check=True)
+    subprocess.run([cxx, "-O1", "-std=c++17", "-ffp-contract=off", "-I" + CLI_SRC, os.path.join(ROOT, "tests", "cli", "png_check.cpp"),
+                    os.path.join(CLI_SRC, "png.cpp"), os.path.join(CLI_SRC, "jpeg.cpp"), "-o", exe], check=True)
     return exe
 
 
@@ -182,6 +184,84 @@ def test_png_decoder_rejects_bad_files(png_check, tmp_path):
         r = subprocess.run([png_check, "read", str(p), str(tmp_path / "x.raw")], capture_output=True, text=True)
         assert r.returncode == 1, name
         assert r.stderr.strip(), name
+
+
+# ---------------------------------------------------------------------------
+# JPEG reading
+# ---------------------------------------------------------------------------
+def _test_image(h, w, grey, seed):
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w]
+    a = np.stack([128 + 100 * np.sin(x / 7 + k) * np.cos(y / 5 - k) for k in range(1 if grey else 3)], -1)
+    a = np.clip(a + rng.normal(0, 6, a.shape), 0, 255).astype(np.uint8)
+    return a[..., 0] if grey else a
+
+
+JPEG_CASES = [  # (height, width, luma sampling, restart interval, 16-bit tables, grey, one DHT segment)
+    (9, 13, (1, 1), 0, False, True, True),
+    (11, 17, (1, 1), 0, False, False, False),
+    (21, 33, (2, 2), 2, False, False, True),
+    (16, 16, (2, 1), 0, True, False, True),
+    (30, 9, (1, 2), 3, False, False, False),
+    (1, 1, (2, 2), 0, False, False, True),
+    (64, 80, (2, 2), 1, False, False, True),
+    (40, 23, (1, 1), 7, True, True, False),
+]
+
+
+@pytest.mark.parametrize("h,w,sampling,restart,q16,grey,one_dht", JPEG_CASES)
+def test_jpeg_decoder_matches_encoder(png_check, tmp_path, h, w, sampling, restart, q16, grey, one_dht):
+    import jpeg_encode
+    img = _test_image(h, w, grey, h * 31 + w)
+    data, expected = jpeg_encode.encode(img, sampling=sampling, restart=restart, q16=q16, one_dht=one_dht)
+    path = tmp_path / "img.jpg"
+    path.write_bytes(data)
+    got, gray = _read(png_check, path, tmp_path)
+    assert gray == grey
+    # float IDCT and colour conversion on both sides: at most a rounding step apart
+    d = np.abs(got.astype(np.int64) - expected.astype(np.int64))
+    assert d.max() <= 1 and d.mean() < 1e-3
+
+
+def test_jpeg_decoder_near_lossless_against_source(png_check, tmp_path):
+    """Unit quantisation tables: the decode comes back to the source image (the colour
+    conversion and block order checked against the pixels, not against the writer's model)."""
+    import jpeg_encode
+    ones = np.ones(64, np.int64)
+    for sampling in [(1, 1), (2, 2)]:
+        img = _test_image(48, 40, False, 1)
+        data, _ = jpeg_encode.encode(img, sampling=sampling, luma_q=ones, chroma_q=ones)
+        path = tmp_path / "img.jpg"
+        path.write_bytes(data)
+        got, _ = _read(png_check, path, tmp_path)
+        mse = np.mean((got.astype(np.float64) - img) ** 2)
+        assert 10 * np.log10(255.0 ** 2 / mse) > (45.0 if sampling == (1, 1) else 28.0)
+
+
+def test_jpeg_decoder_rejects_bad_files(png_check, tmp_path):
+    import jpeg_encode
+    good, _ = jpeg_encode.encode(_test_image(16, 16, False, 2))
+    sof = good.index(b"\xff\xc0")
+    bad = {
+        "progressive": good[:sof + 1] + b"\xc2" + good[sof + 2:],
+        "truncated": good[: len(good) * 2 // 3],
+        "truncated_scan": good[:-12],
+        "precision12": good[:sof + 4] + b"\x0c" + good[sof + 5:],
+        "no_scan": good[: good.index(b"\xff\xda")] + b"\xff\xd9",
+        "too_large": good[:sof + 5] + struct.pack(">HH", 60000, 60000) + good[sof + 9:],
+        # within the size limit, but far more blocks than a few hundred bytes of scan can code
+        "huge": good[:sof + 5] + struct.pack(">HH", 40000, 40000) + good[sof + 9:],
+    }
+    for name, data in bad.items():
+        p = tmp_path / f"{name}.jpg"
+        p.write_bytes(data)
+        r = subprocess.run([png_check, "read", str(p), str(tmp_path / "x.raw")], capture_output=True, text=True)
+        assert r.returncode == 1, name
+        assert r.stderr.strip(), name
+    for name, needle in [("progressive", "progressive"), ("huge", "truncated"), ("truncated_scan", "truncated")]:
+        r = subprocess.run([png_check, "read", str(tmp_path / f"{name}.jpg"), str(tmp_path / "x.raw")],
+                           capture_output=True, text=True)
+        assert needle in r.stderr, (name, r.stderr)
 
 
 # ---------------------------------------------------------------------------

@@ -112,9 +112,13 @@ def test_cli_init_modes_mask_and_ssim(sad_cuda, image, tmp_path):
 def test_run_sh_batch_mode(sad_cuda, tmp_path):
     imgs = tmp_path / "imgs"
     imgs.mkdir()
+    import jpeg_encode
     for i, (w, h) in enumerate([(48, 40), (40, 56)]):
-        img = synthetic_image(w, h, seed=10 + i)
-        imageio.write_png(str(imgs / f"im{i}.png"), np.round(np.clip(img, 0, 1) * 255).astype(np.uint8))
+        img = np.round(np.clip(synthetic_image(w, h, seed=10 + i), 0, 1) * 255).astype(np.uint8)
+        if i == 0:
+            imageio.write_png(str(imgs / f"im{i}.png"), img)
+        else:  # run.sh batches png, jpg and jpeg files
+            (imgs / f"im{i}.jpg").write_bytes(jpeg_encode.encode(img, sampling=(2, 2))[0])
     out = tmp_path / "out"
     r = subprocess.run([os.path.join(ROOT, "run.sh"), str(imgs), "--iters", "30", "--sites", "200",
                         "--log-freq", "10", "--out-dir", str(out)],
@@ -127,6 +131,37 @@ def test_run_sh_batch_mode(sad_cuda, tmp_path):
     assert len(re.findall(r"Active sites: \d+/\d+", text)) == 2
     for i in range(2):
         assert (out / f"im{i}.png").exists() and (out / f"im{i}_sites.txt").exists()
+
+
+def test_cli_fits_jpeg_like_its_decoded_pixels(sad_cuda, tmp_path):
+    """A JPEG input fits exactly like a PNG holding the pixels the host's JPEG reader decodes
+    (read here through tests/cli/png_check.cpp, built from the same reader source)."""
+    import shutil
+    import jpeg_encode
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    src = os.path.join(ROOT, "sad_gb300", "cli")
+    check = str(tmp_path / "png_check")
+    subprocess.run([cxx, "-O1", "-std=c++17", "-ffp-contract=off", "-I" + src,
+                    os.path.join(ROOT, "tests", "cli", "png_check.cpp"), os.path.join(src, "png.cpp"),
+                    os.path.join(src, "jpeg.cpp"), "-o", check], check=True)
+    img = np.round(np.clip(synthetic_image(64, 48, seed=9), 0, 1) * 255).astype(np.uint8)
+    data, model = jpeg_encode.encode(img, sampling=(2, 1))
+    jpg, png, raw = tmp_path / "photo.jpg", tmp_path / "photo_png.png", tmp_path / "photo.raw"
+    jpg.write_bytes(data)
+    subprocess.run([check, "read", str(jpg), str(raw)], check=True)
+    head, body = raw.read_bytes().split(b"\n", 1)
+    decoded = np.frombuffer(body, np.uint8).reshape(48, 64, 3)
+    assert np.abs(decoded.astype(np.int64) - model).max() <= 1
+    imageio.write_png(str(png), decoded)
+    log = _fit(sad_cuda, jpg, tmp_path / "a")
+    assert "image=64x48" in log
+    _fit(sad_cuda, png, tmp_path / "b")
+    a = (tmp_path / "a" / "photo_sites.txt").read_bytes()
+    b = (tmp_path / "b" / "photo_png_sites.txt").read_bytes()
+    assert a == b
+    assert imageio.read_png(str(tmp_path / "a" / "photo.png")).shape == (48, 64, 3)
 
 
 def test_cli_packed_psnr_and_render_packed(sad_cuda, image, tmp_path):
