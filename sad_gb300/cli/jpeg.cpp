@@ -176,18 +176,22 @@ Image8 read_jpeg(const std::string& path) {
         uint16_t len = be16(d, p);
         if (len < 2 || p + len > d.size()) throw std::runtime_error("truncated JPEG segment");
         size_t q = p + 2, end = p + len;
+        // every read of the segment stays inside it
+        auto need = [&](size_t at, size_t n) {
+            if (at + n > end) throw std::runtime_error("truncated JPEG segment");
+        };
         switch (m) {
             case 0xDB:  // DQT
                 while (q < end) {
                     int pq = d[q] >> 4, tq = d[q] & 15;
                     ++q;
                     if (tq > 3) throw std::runtime_error("invalid JPEG quantisation table id");
+                    need(q, pq ? 128 : 64);
                     for (int i = 0; i < 64; ++i) {
                         if (pq) {
                             qt[tq][kZigzag[i]] = be16(d, q);
                             q += 2;
                         } else {
-                            if (q >= end) throw std::runtime_error("truncated JPEG quantisation table");
                             qt[tq][kZigzag[i]] = d[q++];
                         }
                     }
@@ -220,6 +224,7 @@ Image8 read_jpeg(const std::string& path) {
                 break;
             case 0xC0:
             case 0xC1: {  // SOF0 / SOF1
+                need(q, 6);
                 if (d[q] != 8) throw std::runtime_error("JPEG sample precision other than 8 bits is not supported");
                 height = be16(d, q + 1);
                 width = be16(d, q + 3);
@@ -227,7 +232,9 @@ Image8 read_jpeg(const std::string& path) {
                 if (width <= 0 || height <= 0) throw std::runtime_error("JPEG without image size");
                 if (uint64_t(width) * height > (uint64_t(1) << 31)) throw std::runtime_error("JPEG dimensions too large");
                 if (nc != 1 && nc != 3) throw std::runtime_error("JPEG with other than 1 or 3 components");
+                if (frame) throw std::runtime_error("JPEG with more than one frame header");
                 q += 6;
+                need(q, 3 * size_t(nc));
                 for (int i = 0; i < nc; ++i, q += 3) {
                     Component c;
                     c.id = d[q];
@@ -256,11 +263,14 @@ Image8 read_jpeg(const std::string& path) {
             case 0xCF:
                 throw std::runtime_error("progressive, lossless or arithmetic-coded JPEG is not supported");
             case 0xDD:  // DRI
+                need(q, 2);
                 restart = be16(d, q);
                 break;
             case 0xDA: {  // SOS: one interleaved scan holding every component
                 if (!frame) throw std::runtime_error("JPEG scan before frame header");
+                need(q, 1);
                 int ns = d[q++];
+                need(q, 2 * size_t(ns) + 3);
                 if (ns != static_cast<int>(comps.size())) throw std::runtime_error("non-interleaved JPEG scans are not supported");
                 if (ns == 1) {  // a single-component scan codes one block per MCU (T.81 A.2.2)
                     comps[0].h = comps[0].v = 1;

@@ -264,6 +264,39 @@ def test_jpeg_decoder_rejects_bad_files(png_check, tmp_path):
         assert needle in r.stderr, (name, r.stderr)
 
 
+def test_image_readers_survive_corrupted_files(tmp_path):
+    """Truncated and byte-corrupted PNG and JPEG files end in an error message or an image,
+    never in a crash, with the readers built under AddressSanitizer and UBSan."""
+    import jpeg_encode
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    exe = str(tmp_path / "png_check_asan")
+    r = subprocess.run([cxx, "-O1", "-g", "-std=c++17", "-ffp-contract=off", "-fsanitize=address,undefined",
+                        "-fno-sanitize-recover=undefined", "-I" + CLI_SRC,
+                        os.path.join(ROOT, "tests", "cli", "png_check.cpp"), os.path.join(CLI_SRC, "png.cpp"),
+                        os.path.join(CLI_SRC, "jpeg.cpp"), "-o", exe], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("sanitizer runtime not available: " + r.stderr[-200:])
+    rng = np.random.default_rng(0)
+    jpg, _ = jpeg_encode.encode(_test_image(24, 40, False, 3), sampling=(2, 2), restart=2)
+    png = encode_png(rng.integers(0, 256, (20, 30, 3)), 2, 8, rng)
+    f, out = tmp_path / "f.bin", tmp_path / "f.raw"
+    outcomes = {0: 0, 1: 0}
+    for trial in range(300):
+        b = bytearray(jpg if trial % 2 == 0 else png)
+        if trial % 3 == 0:
+            b = b[: rng.integers(2, len(b))]
+        else:
+            for _ in range(rng.integers(1, 6)):
+                b[rng.integers(2, len(b))] = rng.integers(0, 256)
+        f.write_bytes(bytes(b))
+        r = subprocess.run([exe, "read", str(f), str(out)], capture_output=True, text=True)
+        assert r.returncode in (0, 1), (trial, r.returncode, r.stderr[-800:])
+        outcomes[r.returncode] += 1
+    assert outcomes[1] > 0
+
+
 # ---------------------------------------------------------------------------
 # arguments and configuration
 # ---------------------------------------------------------------------------
