@@ -147,6 +147,24 @@ sad_status_t sad_compute_gradients_tiled(
     float ssim_weight, int width, int height, int cand_width, int cand_height,
     sad_stream_t stream);
 
+/* The trainer's form of the same evaluation, the kernel a fit runs every iteration: the
+ * candidate field's 16x16-tile registration, then per-site sums in exact 64-bit fixed
+ * point (value * 2^24, bitwise reproducible).  fix12_out is a zero-initialised device
+ * [site_count][12] int64 buffer receiving the sums: slots 0-9 the gradients in the order
+ * of sad_compute_gradients_tiled's arrays; with compute_removal, slot 10 the removal delta
+ * times *removal_scale_out (a power of two <= 1 chosen for the image size) and slot 11 the
+ * number of pixels whose delta is the 1e6 sentinel (excluded from slot 10).
+ * scratch: sad_compute_gradients_fixed_scratch_bytes(site_count, width, height) bytes.
+ * replaces: launchComputeGradientsTiled, backends/cuda/src/gradients.cu:491-531, as
+ * trainVoronoi calls it each iteration (backends/cuda/src/sad_cuda.cu:2319-2331) */
+size_t sad_compute_gradients_fixed_scratch_bytes(uint32_t site_count, int width, int height);
+sad_status_t sad_compute_gradients_fixed(
+    const uint32_t* cand0, const uint32_t* cand1, const float* target, const float* rendered,
+    const float* mask, const float* sites, float inv_scale_sq, uint32_t site_count,
+    uint32_t compute_removal, float ssim_weight, int width, int height, int cand_width,
+    int cand_height, long long* fix12_out, float* removal_scale_out, void* scratch,
+    size_t scratch_bytes, sad_stream_t stream);
+
 /* One Jacobi pass of the log_tau gradient diffusion.
  * replaces: launchTauDiffuse, backends/cuda/src/tau_diffusion.cu:88-101 */
 sad_status_t sad_tau_diffuse(const uint32_t* cand0, const uint32_t* cand1, const float* sites,

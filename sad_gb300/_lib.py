@@ -84,6 +84,9 @@ SIGNATURES = {
     "sad_pack_jump_step": (u32, [u32, i32, i32]),
     "sad_compute_gradients_tiled": (st, [vp, vp, vp, vp, vp] + [vp] * 10 +
                                     [vp, f32, u32, vp, u32, f32, i32, i32, i32, i32, vp]),
+    "sad_compute_gradients_fixed_scratch_bytes": (sz, [u32, i32, i32]),
+    "sad_compute_gradients_fixed": (st, [vp, vp, vp, vp, vp, vp, f32, u32, u32, f32, i32, i32, i32, i32,
+                                         vp, vp, vp, sz, vp]),
     "sad_tau_diffuse": (st, [vp, vp, vp, vp, vp, vp, u32, f32, i32, i32, i32, vp]),
     "sad_adam_update": (st, [vp, vp] + [vp] * 10 + [f32] * 9 + [u32, u32, i32, i32, vp]),
     "sad_clear_gradients": (st, [vp] * 10 + [u32, vp]),

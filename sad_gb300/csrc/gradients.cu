@@ -621,3 +621,59 @@ extern "C" sad_status_t sad_compute_gradients_tiled(
     launch_gradients_raw(p, reinterpret_cast<const Site*>(sites), as_stream(stream));
     return check_launch("sad_compute_gradients_tiled");
 }
+
+extern "C" size_t sad_compute_gradients_fixed_scratch_bytes(uint32_t site_count, int width, int height) {
+    if (width <= 0 || height <= 0) return 0;
+    auto a256 = [](size_t x) { return (x + 255) & ~size_t(255); };
+    return 256 + a256(size_t(site_count) * sizeof(SiteGeom)) + a256(size_t(site_count) * sizeof(SiteColor)) +
+           a256(tile_map_words(width, height) * sizeof(uint32_t));
+}
+
+extern "C" sad_status_t sad_compute_gradients_fixed(
+    const uint32_t* cand0, const uint32_t* cand1, const float* target, const float* rendered,
+    const float* mask, const float* sites, float inv_scale_sq, uint32_t site_count,
+    uint32_t compute_removal, float ssim_weight, int width, int height, int cand_width,
+    int cand_height, long long* fix12_out, float* removal_scale_out, void* scratch,
+    size_t scratch_bytes, sad_stream_t stream) {
+    clear_error();
+    SAD_REQUIRE(width > 0 && height > 0, "sad_compute_gradients_fixed: invalid image size");
+    SAD_REQUIRE(cand_width > 0 && cand_height > 0, "sad_compute_gradients_fixed: invalid cand size");
+    SAD_REQUIRE(cand0 && cand1 && target && fix12_out, "sad_compute_gradients_fixed: null input");
+    SAD_REQUIRE(ssim_weight <= 0.0f || rendered, "sad_compute_gradients_fixed: SSIM needs rendered");
+    SAD_REQUIRE(sites || site_count == 0, "sad_compute_gradients_fixed: null sites");
+    SAD_REQUIRE(scratch && scratch_bytes >= sad_compute_gradients_fixed_scratch_bytes(site_count, width, height),
+                "sad_compute_gradients_fixed: scratch too small");
+    const float scale = removal_fix_mul(width, height);
+    if (removal_scale_out) *removal_scale_out = scale;
+    cudaStream_t st = as_stream(stream);
+    auto a256 = [](size_t x) { return (x + 255) & ~size_t(255); };
+    char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(scratch) + 255) & ~uintptr_t(255));
+    SiteGeom* geom = reinterpret_cast<SiteGeom*>(p);
+    p += a256(size_t(site_count) * sizeof(SiteGeom));
+    SiteColor* color = reinterpret_cast<SiteColor*>(p);
+    p += a256(size_t(site_count) * sizeof(SiteColor));
+    TileMap map = tile_map_at(reinterpret_cast<uint32_t*>(p), width, height);
+    launch_prepare_sites(reinterpret_cast<const Site*>(sites), geom, color, site_count, st);
+    launch_register_tiles(cand0, cand1, site_count, width, height, cand_width, cand_height, map, st);
+    GradParams g{};
+    g.cand0 = cand0;
+    g.cand1 = cand1;
+    g.target = target;
+    g.rendered = rendered;
+    g.mask = mask;
+    g.inv_scale_sq = inv_scale_sq;
+    g.site_count = site_count;
+    g.ssim_weight = ssim_weight;
+    g.width = width;
+    g.height = height;
+    g.cand_width = cand_width;
+    g.cand_height = cand_height;
+    g.fix12 = fix12_out;
+    g.removal_fix_mul = scale;
+    g.compute_removal = compute_removal ? 1 : 0;
+    g.slot_map = map.slot_map;
+    g.tile_keys = map.tile_keys;
+    g.tile_count = map.tile_count;
+    launch_gradients_prepared(g, geom, color, st);
+    return check_launch("sad_compute_gradients_fixed");
+}

@@ -246,6 +246,64 @@ def test_fused_gradients_match_oracle(ops, orc, w, h, n, removal, masked, ssim):
         assert np.all(np.abs(r - rem) <= 1e-3 * np.maximum(np.abs(rem), 1.0) + 1e-4)
 
 
+def _fixed_gradients(w, h, n, c0, c1, img, rendered, mask, sites, removal, ssim):
+    """The trainer's fixed-point gradient kernel through sad_compute_gradients_fixed:
+    (int64 [N,12] sums, removal scale)."""
+    import ctypes as C
+    from sad_gb300 import _lib
+    lib = _lib.load()
+    nb = lib.sad_compute_gradients_fixed_scratch_bytes(n, w, h)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    out = torch.zeros((n, 12), dtype=torch.int64, device="cuda")
+    keep = [t32(c0), t32(c1), tf(img), tf(rendered), tf(mask), tf(sites)]
+    scale = C.c_float(0.0)
+    st = lib.sad_compute_gradients_fixed(*[C.c_void_p(t.data_ptr()) for t in keep], 1.0 / max(w, h) ** 2, n,
+                                         int(removal), ssim, w, h, w, h, C.c_void_p(out.data_ptr()),
+                                         C.byref(scale), C.c_void_p(scratch.data_ptr()), nb, None)
+    assert st == 0, lib.sad_last_error()
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), scale.value
+
+
+@pytest.mark.parametrize("w,h,n,field,removal,masked,ssim", [
+    (64, 64, 400, "random", False, False, 0.0), (97, 61, 900, "random", True, False, 0.0),
+    (128, 128, 2000, "knn", True, True, 0.0), (72, 40, 300, "knn", False, False, 0.2),
+    (96, 80, 6000, "knn", False, False, 0.0)])
+def test_trainer_gradients_match_oracle(ops, orc, w, h, n, field, removal, masked, ssim):
+    """The trainer's kernel (precomputed tile registration, sites staged in shared memory,
+    fixed-point sums) against the oracle and against the float API kernel on the same
+    inputs.  The random fields put far more than a tile table's 256 keys in each 16x16 tile
+    (the global path) and repeat ids within lists; the k-nearest fields are what a fit
+    sees, and at 6000 sites on 96x80 they too overflow the tables.  (A random field that
+    dense is not used against the oracle: its far candidates give single-pixel terms of
+    ~1e-6 whose FP32 value, identical in both GPU kernels, is ill-conditioned.)  Fixed
+    point: the same sums to the last bit on a second run."""
+    img, sites = cases.scene(w, h, n, 40 + n)
+    sites[::9, 0] = -1
+    c0, c1 = cases.random_field(w, h, n, 41) if field == "random" else cases.knn_field(sites, w, h)
+    mask = np.ones((h, w), np.float32)
+    if masked:
+        mask[h // 3: h // 2, :] = 0.0
+    rendered = orc.render(c0, c1, sites, w, h)
+    fix, scale = _fixed_gradients(w, h, n, c0, c1, img, rendered, mask, sites, removal, ssim)
+    again, _ = _fixed_gradients(w, h, n, c0, c1, img, rendered, mask, sites, removal, ssim)
+    np.testing.assert_array_equal(fix, again)
+    got = fix[:, :10].T.astype(np.float64) / 2.0 ** 24
+    g, a, rem = orc.compute_gradients(c0, c1, img, sites, w, h, mask=mask if masked else None,
+                                      rendered=rendered, ssim_weight=ssim, removal=removal)
+    assert_grads_close(got, g, a)
+    bufs = _grad_buffers(n)
+    ops.compute_gradients_tiled(t32(c0), t32(c1), tf(img), tf(rendered), tf(mask), tf(sites), *bufs,
+                                1.0 / max(w, h) ** 2, 0, int(removal), ssim, w, h)
+    api = np.stack([b.cpu().numpy() for b in bufs[:10]]).astype(np.float64)
+    assert_grads_close(got, api, a)
+    if removal:
+        r = fix[:, 10].astype(np.float64) / 2.0 ** 24 / scale + fix[:, 11] * 1.0e6
+        assert np.all(np.abs(r - rem) <= 1e-3 * np.maximum(np.abs(rem), 1.0) + 1e-4)
+    else:
+        assert not fix[:, 10:].any()
+
+
 def test_tau_diffuse_matches_oracle(ops, orc):
     w, h, n = 64, 48, 700
     img, sites = cases.scene(w, h, n, 30)
