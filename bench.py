@@ -186,7 +186,7 @@ def run_ours(args):
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": profiled_kernel().get("dram_bytes_per_launch"),
                 "limiter": profiled_kernel().get("limiter"),
-                "kernel": "fused_gradients_kernel", "launch_ms": round(grad_ms, 5),
+                "kernel": "fused_gradients_pre_kernel", "launch_ms": round(grad_ms, 5),
                 "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
 
     # e2e: host image in pinned memory -> fit -> active sites + PSNR back
