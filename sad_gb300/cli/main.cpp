@@ -1,15 +1,15 @@
 // main.cpp -- sad_cuda: the command-line host of the reference's CUDA backend
 // (backends/cuda/src/sad_cuda.cu) rebuilt on libsad_gb300's C ABI.
 //
-//   sad_cuda <image.png> [training options]     fit; writes <out-dir>/<stem>.png and
+//   sad_cuda <image.png|jpg> [training options] fit; writes <out-dir>/<stem>.png and
 //                                                <out-dir>/<stem>_sites.txt
 //   sad_cuda --render <sites.txt|json> [opts]   render; writes <sites>_render.png
 //
 // Same flags, defaults ($CONFIG_PATH or ./training_config.json, required) and exit codes as the
 // reference (sad_cuda.cu:459-517 defaults, 754-895 flags, unknown flag -> exit 1); the log
 // lines keep the reference's layout.
-// Images are PNG (the reference reads any stb format); an image larger than MAX_DIM is
-// box-filtered down.
+// Images are PNG or baseline JPEG (the reference reads any stb format); an image larger
+// than MAX_DIM is box-filtered down.
 #include <cuda_runtime.h>
 
 #include <algorithm>
