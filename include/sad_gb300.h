@@ -46,7 +46,8 @@ typedef enum {
     SAD_ERR_CUDA = 2,
     SAD_ERR_OUT_OF_MEMORY = 3,
     SAD_ERR_UNSUPPORTED = 4,
-    SAD_ERR_INTERNAL = 5
+    SAD_ERR_INTERNAL = 5,
+    SAD_ERR_CANCELLED = 6   /* an executor request withdrawn before it started */
 } sad_status_t;
 
 /* ------------------------------------------------------------------------ */
@@ -557,6 +558,14 @@ sad_status_t sad_executor_submit_render(sad_executor_t* ex, const sad_render_con
                                         uint64_t* ticket);
 sad_status_t sad_executor_wait(sad_executor_t* ex, uint64_t ticket);
 sad_status_t sad_executor_wait_all(sad_executor_t* ex);
+/* Withdraw a queued request.  *cancelled = 1 when it had not started: it is removed, its
+ * result has status SAD_ERR_CANCELLED and its host buffers are released at once;
+ * *cancelled = 0 when it has started or finished (it then completes as submitted). */
+sad_status_t sad_executor_cancel(sad_executor_t* ex, uint64_t ticket, int* cancelled);
+/* Failure testing without a GPU fault: the next `count` slab allocations are refused on the
+ * host, as if the memory pool were exhausted (SAD_ERR_OUT_OF_MEMORY on those requests; no
+ * CUDA call is made for them).  The executor keeps serving the requests after them. */
+sad_status_t sad_executor_inject_slab_failures(sad_executor_t* ex, int count);
 /* Runs what is queued, then joins the workers. */
 sad_status_t sad_executor_destroy(sad_executor_t* ex);
 

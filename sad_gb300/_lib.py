@@ -146,6 +146,8 @@ SIGNATURES = {
                                         C.POINTER(RequestResult), C.POINTER(C.c_uint64)]),
     "sad_executor_wait": (st, [vp, C.c_uint64]),
     "sad_executor_wait_all": (st, [vp]),
+    "sad_executor_cancel": (st, [vp, C.c_uint64, C.POINTER(i32)]),
+    "sad_executor_inject_slab_failures": (st, [vp, i32]),
     "sad_executor_destroy": (st, [vp]),
 }
 

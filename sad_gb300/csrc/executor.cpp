@@ -70,6 +70,7 @@ struct sad_executor {
     size_t in_use = 0;
     int max_fits = 0;   // 0: no limit
     int running_fits = 0;
+    int inject_slab_failures = 0;  // host-side refusals still to make (failure tests)
     bool stop = false;
     uint64_t next_ticket = 1;
     std::deque<Request> queue;
@@ -120,6 +121,7 @@ void worker_main(sad_executor* ex) {
     const std::string setup_error = setup == SAD_OK ? std::string() : std::string(sad_last_error());
     for (;;) {
         Request q;
+        bool refused = false;  // slab refused by failure injection
         {
             std::unique_lock<std::mutex> lock(ex->mu);
             // the earliest queued request that fits the memory budget and, for a fit, the
@@ -140,6 +142,10 @@ void worker_main(sad_executor* ex) {
             ex->queue.erase(it);
             ex->in_use += q.need;
             if (q.kind == 0) ++ex->running_fits;
+            if (ex->inject_slab_failures > 0) {
+                --ex->inject_slab_failures;
+                refused = true;
+            }
         }
         sad_request_result_t* r = q.result;
         Clock::time_point start = Clock::now();
@@ -148,6 +154,10 @@ void worker_main(sad_executor* ex) {
         void* mem = nullptr;
         sad_status_t st = setup;
         if (st != SAD_OK) sad::set_error("%s", setup_error.c_str());
+        if (st == SAD_OK && refused) {
+            sad::set_error("executor: slab allocation refused (injected failure)");
+            st = SAD_ERR_OUT_OF_MEMORY;
+        }
         if (st == SAD_OK) st = sad::check_cuda(cudaMallocAsync(&mem, q.need, ws), "executor: slab allocation");
         if (st == SAD_OK) st = sad::check_cuda(cudaStreamSynchronize(ws), "executor: slab allocation");
         if (st == SAD_OK) st = q.kind == 0 ? run_fit(q, mem, r) : run_render(q, mem, ws);
@@ -280,6 +290,38 @@ extern "C" sad_status_t sad_executor_wait_all(sad_executor_t* ex) {
     SAD_REQUIRE(ex, "sad_executor_wait_all: null executor");
     std::unique_lock<std::mutex> lock(ex->mu);
     ex->cv_done.wait(lock, [&] { return ex->inflight.empty(); });
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_executor_cancel(sad_executor_t* ex, uint64_t ticket, int* cancelled) {
+    sad::clear_error();
+    SAD_REQUIRE(ex && cancelled, "sad_executor_cancel: null argument");
+    *cancelled = 0;
+    {
+        std::lock_guard<std::mutex> lock(ex->mu);
+        SAD_REQUIRE(ticket > 0 && ticket < ex->next_ticket, "sad_executor_cancel: unknown ticket");
+        auto it = std::find_if(ex->queue.begin(), ex->queue.end(),
+                               [&](const Request& q) { return q.ticket == ticket; });
+        if (it == ex->queue.end()) return SAD_OK;  // running or done
+        sad_request_result_t* r = it->result;
+        r->status = SAD_ERR_CANCELLED;
+        std::strncpy(r->message, "cancelled before it started", sizeof(r->message) - 1);
+        r->message[sizeof(r->message) - 1] = '\0';
+        r->queue_ms = std::chrono::duration<double, std::milli>(Clock::now() - it->submitted).count();
+        ex->queue.erase(it);
+        ex->inflight.erase(ticket);
+        *cancelled = 1;
+    }
+    ex->cv_done.notify_all();
+    ex->cv_work.notify_all();  // the new queue head may fit where the withdrawn one did not
+    return SAD_OK;
+}
+
+extern "C" sad_status_t sad_executor_inject_slab_failures(sad_executor_t* ex, int count) {
+    sad::clear_error();
+    SAD_REQUIRE(ex && count >= 0, "sad_executor_inject_slab_failures: invalid argument");
+    std::lock_guard<std::mutex> lock(ex->mu);
+    ex->inject_slab_failures = count;
     return SAD_OK;
 }
 

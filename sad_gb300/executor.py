@@ -108,6 +108,20 @@ class Executor:
         self._pending[req.ticket.value] = req
         return req
 
+    def cancel(self, req: _Request) -> bool:
+        """Withdraw a request that has not started (True); one that has started or finished
+        completes as submitted (False).  A withdrawn request's result() raises RequestError."""
+        flag = C.c_int(0)
+        self._check(self._lib.sad_executor_cancel(self._h, req.ticket, C.byref(flag)))
+        if flag.value:
+            req._done = True
+            self._pending.pop(req.ticket.value, None)
+        return bool(flag.value)
+
+    def inject_slab_failures(self, count: int) -> None:
+        """Failure testing: refuse the next `count` slab allocations on the host (no GPU fault)."""
+        self._check(self._lib.sad_executor_inject_slab_failures(self._h, count))
+
     def wait_all(self) -> None:
         self._check(self._lib.sad_executor_wait_all(self._h))
         for req in self._pending.values():

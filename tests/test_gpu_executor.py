@@ -167,3 +167,55 @@ def test_executor_fit_cap_lets_renders_pass(cuda):
         want_r = solo_render(sites, 128, 96)
         for r in renders:
             np.testing.assert_array_equal(r.result(), want_r)
+
+
+
+def test_executor_cancel_queued_request(cuda):
+    """A request still queued behind a running fit is withdrawn: its result reports the
+    cancellation, and the requests around it complete with their solo results."""
+    from sad_gb300.executor import Executor, RequestError
+    imgs = [cases.scene(96, 80, 80 + i)[0] for i in range(3)]
+    cfg = small_cfg(iterations=200)
+    with Executor(workers=1) as ex:  # one worker: requests run strictly one after another
+        first = ex.submit_fit(imgs[0], config=cfg)
+        withdrawn = ex.submit_fit(imgs[1], config=cfg)
+        last = ex.submit_fit(imgs[2], config=cfg)
+        assert ex.cancel(withdrawn)
+        with pytest.raises(RequestError, match="cancelled"):
+            withdrawn.result()
+        assert withdrawn.res.status == 6  # SAD_ERR_CANCELLED
+        ex.wait_all()
+        assert not ex.cancel(first)  # finished: nothing to withdraw
+        for req, img in ((first, imgs[0]), (last, imgs[2])):
+            sites_out, psnr = req.result()
+            want, want_psnr = solo_fit(img, cfg)
+            assert psnr == want_psnr
+            np.testing.assert_array_equal(sites_out, want)
+
+
+def test_executor_survives_refused_slabs(cuda):
+    """Host-side failure injection (no GPU fault): refused slab allocations fail exactly
+    their requests with an out-of-memory status and release their budget; the executor
+    keeps serving, and the other requests give their solo results."""
+    from sad_gb300.executor import Executor, RequestError
+    _, sites = cases.scene(96, 64, 90)
+    want = solo_render(sites, 96, 64)
+    budget = 1 << 30
+    with Executor(workers=2, hbm_budget_bytes=budget) as ex:
+        ex.inject_slab_failures(2)
+        reqs = [ex.submit_render(sites, 96, 64) for _ in range(6)]
+        ex.wait_all()
+        failed = [r for r in reqs if r.res.status != 0]
+        assert len(failed) == 2
+        for r in failed:
+            assert r.res.status == 3  # SAD_ERR_OUT_OF_MEMORY
+            with pytest.raises(RequestError, match="injected"):
+                r.result()
+        for r in reqs:
+            if r.res.status == 0:
+                np.testing.assert_array_equal(r.result(), want)
+        # the refused requests' budget was released: a full-budget sequence still runs
+        more = [ex.submit_render(sites, 96, 64) for _ in range(3)]
+        ex.wait_all()
+        for r in more:
+            np.testing.assert_array_equal(r.result(), want)
