@@ -116,8 +116,15 @@ void worker_main(sad_executor* ex) {
     // each with that error, so no waiter is left behind
     cudaStream_t ws = nullptr;
     sad_status_t setup = sad::check_cuda(cudaSetDevice(ex->device), "executor worker: device");
+    // the worker's own stream (renders, slab allocation) at the device's highest priority:
+    // a render's blocks are scheduled ahead of pending fit blocks as SMs free up, so a
+    // short render is not queued behind a fit's kernels
+    int least = 0, greatest = 0;
     if (setup == SAD_OK)
-        setup = sad::check_cuda(cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking), "executor worker: stream");
+        setup = sad::check_cuda(cudaDeviceGetStreamPriorityRange(&least, &greatest), "executor worker: priorities");
+    if (setup == SAD_OK)
+        setup = sad::check_cuda(cudaStreamCreateWithPriority(&ws, cudaStreamNonBlocking, greatest),
+                                "executor worker: stream");
     const std::string setup_error = setup == SAD_OK ? std::string() : std::string(sad_last_error());
     for (;;) {
         Request q;
