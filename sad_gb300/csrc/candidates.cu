@@ -452,7 +452,7 @@ extern "C" sad_status_t sad_jfa_seed(uint32_t* cand0, const float* sites, uint32
                                      int width, int height, int cand_downscale,
                                      sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_jfa_seed: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_jfa_seed: invalid cand size");
     SAD_REQUIRE(cand0 && (sites || site_count == 0), "sad_jfa_seed: null buffer");
     launch_jfa_seed(cand0, reinterpret_cast<const Site*>(sites), site_count, width, height,
                     cand_downscale, as_stream(stream));
@@ -465,7 +465,7 @@ extern "C" sad_status_t sad_jfa_flood(const uint32_t* in_cand0, uint32_t* out_ca
                                       int cand_downscale, int target_width, int target_height,
                                       sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_jfa_flood: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_jfa_flood: invalid cand size");
     SAD_REQUIRE(target_width > 0 && target_height > 0, "sad_jfa_flood: invalid target size");
     SAD_REQUIRE(in_cand0 && out_cand0 && (sites || site_count == 0), "sad_jfa_flood: null buffer");
     SAD_REQUIRE(in_cand0 != out_cand0, "sad_jfa_flood: in and out must differ");
@@ -483,7 +483,7 @@ extern "C" sad_status_t sad_update_candidates(
     uint32_t hilbert_window, int cand_downscale, int target_width, int target_height, int width,
     int height, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_update_candidates: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_update_candidates: invalid cand size");
     SAD_REQUIRE(target_width > 0 && target_height > 0, "sad_update_candidates: invalid target size");
     SAD_REQUIRE(in_cand0 && in_cand1 && out_cand0 && out_cand1, "sad_update_candidates: null field");
     SAD_REQUIRE(in_cand0 != out_cand0 && in_cand1 != out_cand1,

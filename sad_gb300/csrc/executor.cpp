@@ -267,7 +267,7 @@ extern "C" sad_status_t sad_executor_submit_render(sad_executor_t* ex, const sad
                                                    uint64_t* ticket) {
     sad::clear_error();
     SAD_REQUIRE(ex && cfg && sites_host && rgb_host && result, "sad_executor_submit_render: null argument");
-    SAD_REQUIRE(site_count > 0 && width > 0 && height > 0, "sad_executor_submit_render: no sites or empty image");
+    SAD_REQUIRE(site_count > 0 && sad::image_size_ok(width, height), "sad_executor_submit_render: no sites or invalid image size");
     SAD_REQUIRE(cfg->candidate_passes >= 0, "sad_executor_submit_render: negative candidate passes");
     std::memset(result, 0, sizeof(*result));
     Request q;

@@ -590,8 +590,8 @@ extern "C" sad_status_t sad_compute_gradients_tiled(
     float ssim_weight, int width, int height, int cand_width, int cand_height,
     sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_compute_gradients_tiled: invalid image size");
-    SAD_REQUIRE(cand_width > 0 && cand_height > 0, "sad_compute_gradients_tiled: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_compute_gradients_tiled: invalid image size");
+    SAD_REQUIRE(image_size_ok(cand_width, cand_height), "sad_compute_gradients_tiled: invalid cand size");
     SAD_REQUIRE(cand0 && cand1 && target, "sad_compute_gradients_tiled: null input");
     SAD_REQUIRE(ssim_weight <= 0.0f || rendered, "sad_compute_gradients_tiled: SSIM needs rendered");
     SAD_REQUIRE(grad_pos_x && grad_pos_y && grad_log_tau && grad_radius && grad_color_r &&
@@ -623,7 +623,7 @@ extern "C" sad_status_t sad_compute_gradients_tiled(
 }
 
 extern "C" size_t sad_compute_gradients_fixed_scratch_bytes(uint32_t site_count, int width, int height) {
-    if (width <= 0 || height <= 0) return 0;
+    if (!image_size_ok(width, height)) return 0;
     auto a256 = [](size_t x) { return (x + 255) & ~size_t(255); };
     return 256 + a256(size_t(site_count) * sizeof(SiteGeom)) + a256(size_t(site_count) * sizeof(SiteColor)) +
            a256(tile_map_words(width, height) * sizeof(uint32_t));
@@ -636,8 +636,8 @@ extern "C" sad_status_t sad_compute_gradients_fixed(
     int cand_height, long long* fix12_out, float* removal_scale_out, void* scratch,
     size_t scratch_bytes, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_compute_gradients_fixed: invalid image size");
-    SAD_REQUIRE(cand_width > 0 && cand_height > 0, "sad_compute_gradients_fixed: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_compute_gradients_fixed: invalid image size");
+    SAD_REQUIRE(image_size_ok(cand_width, cand_height), "sad_compute_gradients_fixed: invalid cand size");
     SAD_REQUIRE(cand0 && cand1 && target && fix12_out, "sad_compute_gradients_fixed: null input");
     SAD_REQUIRE(ssim_weight <= 0.0f || rendered, "sad_compute_gradients_fixed: SSIM needs rendered");
     SAD_REQUIRE(sites || site_count == 0, "sad_compute_gradients_fixed: null sites");

@@ -43,6 +43,14 @@ inline sad_status_t check_cuda(cudaError_t e, const char* what) {
 
 inline cudaStream_t as_stream(sad_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Largest image (or candidate field) the kernels address: a pixel's RGB offset, 3 * pixel,
+// is a 32-bit int, so at most floor((2^31 - 1) / 3) pixels (e.g. 26,754 x 26,754).  Larger
+// sizes are rejected as invalid arguments instead of overflowing an index.
+constexpr long long kMaxPixels = 715827882;
+inline bool image_size_ok(int w, int h) {
+    return w > 0 && h > 0 && static_cast<long long>(w) * h <= kMaxPixels;
+}
+
 inline unsigned blocks_for(size_t n, unsigned threads) {
     return static_cast<unsigned>((n + threads - 1) / threads);
 }

@@ -444,7 +444,7 @@ extern "C" sad_status_t sad_tau_diffuse(const uint32_t* cand0, const uint32_t* c
                                         float lambda, int width, int height, int cand_downscale,
                                         sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_tau_diffuse: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_tau_diffuse: invalid cand size");
     SAD_REQUIRE(site_count == 0 || (cand0 && cand1 && sites && grad_raw && grad_in && grad_out),
                 "sad_tau_diffuse: null buffer");
     SAD_REQUIRE(grad_in != grad_out, "sad_tau_diffuse: grad_in and grad_out must differ");
@@ -463,7 +463,7 @@ extern "C" sad_status_t sad_adam_update(float* sites, float* adam, const float* 
                                         float beta2, float eps, uint32_t t, uint32_t site_count,
                                         int width, int height, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_adam_update: invalid image size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_adam_update: invalid image size");
     SAD_REQUIRE(site_count == 0 || (sites && adam && gpx && gpy && glt && grad && gr && gg && gb &&
                                     gdx && gdy && gla),
                 "sad_adam_update: null buffer");

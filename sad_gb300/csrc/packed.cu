@@ -211,7 +211,7 @@ extern "C" sad_status_t sad_pack_inference_sites(const float* sites, uint32_t si
                                                  int height, uint32_t* packed, sad_packed_quant_t* quant,
                                                  sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_pack_inference_sites: invalid size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_pack_inference_sites: invalid size");
     SAD_REQUIRE(width <= 32768 && height <= 32768, "sad_pack_inference_sites: image side above 32768");
     SAD_REQUIRE(quant && (site_count == 0 || (sites && packed)), "sad_pack_inference_sites: null buffer");
     launch_pack_inference(reinterpret_cast<const Site*>(sites), site_count, width, height,
@@ -223,7 +223,7 @@ extern "C" sad_status_t sad_unpack_inference_sites(const uint32_t* packed, const
                                                    uint32_t site_count, int width, int height, float* sites,
                                                    sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_unpack_inference_sites: invalid size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_unpack_inference_sites: invalid size");
     SAD_REQUIRE(site_count == 0 || (packed && quant && sites), "sad_unpack_inference_sites: null buffer");
     launch_unpack_inference(packed, reinterpret_cast<const float*>(quant), site_count, width, height,
                             reinterpret_cast<Site*>(sites), as_stream(stream));
@@ -235,7 +235,7 @@ extern "C" sad_status_t sad_render_packed(const uint32_t* cand0, const uint32_t*
                                           float inv_scale_sq, uint32_t site_count, int width, int height,
                                           int cand_width, int cand_height, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0 && cand_width > 0 && cand_height > 0,
+    SAD_REQUIRE(image_size_ok(width, height) && image_size_ok(cand_width, cand_height),
                 "sad_render_packed: invalid size");
     SAD_REQUIRE(cand0 && cand1 && out_rgb && quant && (site_count == 0 || packed),
                 "sad_render_packed: null buffer");
@@ -259,7 +259,7 @@ extern "C" sad_status_t sad_render_packed_from_sites(const sad_render_config_t* 
                                                      size_t scratch_bytes, sad_stream_t stream) {
     clear_error();
     SAD_REQUIRE(cfg, "sad_render_packed_from_sites: null config");
-    SAD_REQUIRE(width > 0 && height > 0, "sad_render_packed_from_sites: invalid size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_render_packed_from_sites: invalid size");
     SAD_REQUIRE(site_count > 0 && packed && quant && out_rgb && scratch,
                 "sad_render_packed_from_sites: null buffer or no sites");
     SAD_REQUIRE(scratch_bytes >= sad_render_packed_scratch_bytes(site_count, width, height, cfg->cand_downscale),

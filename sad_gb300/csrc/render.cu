@@ -335,8 +335,8 @@ extern "C" sad_status_t sad_render(const uint32_t* cand0, const uint32_t* cand1,
                                    int width, int height, int cand_width, int cand_height,
                                    sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_render: width/height must be positive");
-    SAD_REQUIRE(cand_width > 0 && cand_height > 0, "sad_render: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_render: invalid image size");
+    SAD_REQUIRE(image_size_ok(cand_width, cand_height), "sad_render: invalid cand size");
     SAD_REQUIRE(cand0 && cand1 && out_rgb, "sad_render: null buffer");
     SAD_REQUIRE(sites || site_count == 0, "sad_render: null sites");
     launch_render_raw(cand0, cand1, out_rgb, reinterpret_cast<const Site*>(sites), inv_scale_sq,
@@ -350,8 +350,8 @@ extern "C" sad_status_t sad_render_backward(const uint32_t* cand0, const uint32_
                                             uint32_t site_count, int width, int height,
                                             int cand_width, int cand_height, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_render_backward: width/height must be positive");
-    SAD_REQUIRE(cand_width > 0 && cand_height > 0, "sad_render_backward: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_render_backward: invalid image size");
+    SAD_REQUIRE(image_size_ok(cand_width, cand_height), "sad_render_backward: invalid cand size");
     SAD_REQUIRE(cand0 && cand1 && grad_rgb && grad_sites, "sad_render_backward: null buffer");
     SAD_REQUIRE(sites || site_count == 0, "sad_render_backward: null sites");
     launch_render_backward_raw(cand0, cand1, grad_rgb, grad_sites,
@@ -364,7 +364,7 @@ extern "C" sad_status_t sad_init_candidates(uint32_t* cand0, uint32_t* cand1, ui
                                             uint32_t seed, int per_pixel, int width, int height,
                                             sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_init_candidates: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_init_candidates: invalid cand size");
     SAD_REQUIRE(cand0 && cand1, "sad_init_candidates: null buffer");
     launch_init_candidates(cand0, cand1, site_count, seed, per_pixel, width, height,
                            as_stream(stream));
@@ -374,7 +374,7 @@ extern "C" sad_status_t sad_init_candidates(uint32_t* cand0, uint32_t* cand1, ui
 extern "C" sad_status_t sad_clear_candidates(uint32_t* cand0, uint32_t* cand1, int width,
                                              int height, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_clear_candidates: invalid cand size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_clear_candidates: invalid cand size");
     SAD_REQUIRE(cand0 && cand1, "sad_clear_candidates: null buffer");
     launch_clear_candidates(cand0, cand1, width, height, as_stream(stream));
     return check_launch("sad_clear_candidates");

@@ -72,7 +72,7 @@ static sad_status_t render_from_sites_impl(const sad_render_config_t* cfg, const
                                            int width, int height, float* out_rgb, void* scratch,
                                            size_t scratch_bytes, sad_stream_t stream, cudaEvent_t* ev) {
     SAD_REQUIRE(cfg, "sad_render_from_sites: null config");
-    SAD_REQUIRE(width > 0 && height > 0, "sad_render_from_sites: invalid size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_render_from_sites: invalid size");
     SAD_REQUIRE(n > 0 && sites_f && out_rgb && scratch, "sad_render_from_sites: null buffer or no sites");
     SAD_REQUIRE(cfg->candidate_passes >= 0, "sad_render_from_sites: negative candidate passes");
     int ds = std::max(1, cfg->cand_downscale);

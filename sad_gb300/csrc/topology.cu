@@ -978,7 +978,7 @@ extern "C" sad_status_t sad_split_sites(float* sites, float* adam, const uint32_
                                         uint32_t current_site_count, const float* target,
                                         int width, int height, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_split_sites: invalid image size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_split_sites: invalid image size");
     SAD_REQUIRE(num_to_split == 0 || (sites && adam && split_indices && mass && err_w && err_wx &&
                                       err_wy && err_wxx && err_wxy && err_wyy && target),
                 "sad_split_sites: null buffer");
@@ -998,7 +998,7 @@ extern "C" sad_status_t sad_compute_site_stats(const uint32_t* cand0, const uint
                                                int width, int height, int cand_width,
                                                int cand_height, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0 && cand_width > 0 && cand_height > 0,
+    SAD_REQUIRE(image_size_ok(width, height) && image_size_ok(cand_width, cand_height),
                 "sad_compute_site_stats: invalid size");
     SAD_REQUIRE(cand0 && cand1 && target && (sites || site_count == 0),
                 "sad_compute_site_stats: null input");
@@ -1020,7 +1020,7 @@ extern "C" sad_status_t sad_init_gradient_weighted(float* sites, uint32_t site_c
                                                    int width, int height, void* temp,
                                                    size_t temp_bytes, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_init_gradient_weighted: invalid image size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_init_gradient_weighted: invalid image size");
     SAD_REQUIRE(site_count == 0 || (sites && target && temp), "sad_init_gradient_weighted: null buffer");
     SAD_REQUIRE(site_count == 0 || temp_bytes >= init_temp_bytes(site_count),
                 "sad_init_gradient_weighted: temp smaller than sad_init_temp_bytes(site_count)");
@@ -1065,7 +1065,7 @@ extern "C" sad_status_t sad_compute_mse(const float* rendered, const float* targ
                                         const float* mask, float* mse_accum, int width,
                                         int height, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_compute_mse: invalid size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_compute_mse: invalid size");
     SAD_REQUIRE(rendered && target && mse_accum, "sad_compute_mse: null buffer");
     launch_mse(rendered, target, mask, mse_accum, width, height, as_stream(stream));
     return check_launch("sad_compute_mse");
@@ -1075,7 +1075,7 @@ extern "C" sad_status_t sad_compute_ssim(const float* rendered, const float* tar
                                          const float* mask, float* ssim_accum, int width,
                                          int height, sad_stream_t stream) {
     clear_error();
-    SAD_REQUIRE(width > 0 && height > 0, "sad_compute_ssim: invalid size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_compute_ssim: invalid size");
     SAD_REQUIRE(rendered && target && ssim_accum, "sad_compute_ssim: null buffer");
     launch_ssim(rendered, target, mask, ssim_accum, width, height, as_stream(stream));
     return check_launch("sad_compute_ssim");

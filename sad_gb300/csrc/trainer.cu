@@ -372,7 +372,7 @@ using namespace sad;
 // Sizes and schedule constants of a fit (no device work).
 static sad_status_t plan_trainer(sad_trainer* t, const sad_train_config_t* cfg, int width, int height) {
     SAD_REQUIRE(cfg, "sad_trainer_create: null argument");
-    SAD_REQUIRE(width > 0 && height > 0, "sad_trainer_create: invalid image size");
+    SAD_REQUIRE(image_size_ok(width, height), "sad_trainer_create: invalid image size");
     SAD_REQUIRE(cfg->iterations >= 0, "sad_trainer_create: negative iterations");
     SAD_REQUIRE(cfg->n_sites > 0, "sad_trainer_create: n_sites must be positive");
     SAD_REQUIRE(cfg->cand_update_passes >= 0, "sad_trainer_create: negative candidate passes");

@@ -58,8 +58,18 @@ def test_hilbert_bits_match(sadlib, orc):
 
 def test_argument_errors_are_reported_without_a_device(sadlib):
     from sad_gb300 import _lib
-    with pytest.raises(_lib.SadError, match="width/height"):
+    with pytest.raises(_lib.SadError, match="invalid image size"):
         _lib.call("sad_render", None, None, None, None, 1.0, 0, 0, 0, 1, 1, None)
+    # beyond the kernels' 32-bit pixel offsets (3 * pixel): rejected, not overflowed
+    big = 26755
+    with pytest.raises(_lib.SadError, match="invalid image size"):
+        _lib.call("sad_render", C.c_void_p(64), C.c_void_p(64), C.c_void_p(64), C.c_void_p(64), 1.0, 1,
+                  big, big, 4, 4, None)
+    assert sadlib.sad_compute_gradients_fixed_scratch_bytes(1000, big, big) == 0
+    assert sadlib.sad_compute_gradients_fixed_scratch_bytes(1000, 26754, 26754) > 0
+    cfg = _lib.TrainConfig()
+    sadlib.sad_train_config_default(C.byref(cfg))
+    assert sadlib.sad_trainer_memory_bytes(C.byref(cfg), big, big) == 0
     with pytest.raises(_lib.SadError, match="null buffer"):
         _lib.call("sad_render", None, None, None, None, 1.0, 0, 4, 4, 4, 4, None)
     with pytest.raises(_lib.SadError, match="temp smaller"):
