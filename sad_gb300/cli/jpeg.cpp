@@ -4,7 +4,8 @@
 // components with sampling factors 1-2, restart intervals.  Decoding per T.81 Annex F:
 // canonical Huffman codes from DHT, DC prediction per component, run-length AC
 // coefficients in zig-zag order, dequantisation, a separable float 8x8 inverse DCT, level
-// shift and clamping; chroma planes are replicated to full resolution; JFIF YCbCr -> RGB.
+// shift and clamping; half-resolution chroma brought up by a triangle filter (the IJG
+// decoder's default upsampling); JFIF YCbCr -> RGB.
 // Progressive and arithmetic-coded files are rejected with a message.
 #include <algorithm>
 #include <array>
@@ -312,8 +313,10 @@ Image8 read_jpeg(const std::string& path) {
                                     float blk[64] = {};
                                     int t = decode_symbol(br, dc[c.td]);
                                     if (t > 11) throw std::runtime_error("invalid JPEG DC category");
-                                    c.dc_pred += extend(br.bits(t), t);
-                                    blk[0] = static_cast<float>(c.dc_pred * qt[c.tq][0]);
+                                    // a valid stream keeps the prediction within +-2^11;
+                                    // the clamp only bounds what a corrupt one can build up
+                                    c.dc_pred = std::clamp(c.dc_pred + extend(br.bits(t), t), -(1 << 20), 1 << 20);
+                                    blk[0] = static_cast<float>(c.dc_pred) * static_cast<float>(qt[c.tq][0]);
                                     for (int k = 1; k < 64;) {
                                         int rs = decode_symbol(br, ac[c.ta]);
                                         int r = rs >> 4, s = rs & 15;
@@ -325,7 +328,7 @@ Image8 read_jpeg(const std::string& path) {
                                         k += r;
                                         if (k > 63) throw std::runtime_error("JPEG coefficient index beyond the block");
                                         int zz = kZigzag[k];
-                                        blk[zz] = static_cast<float>(extend(br.bits(s), s) * qt[c.tq][zz]);
+                                        blk[zz] = static_cast<float>(extend(br.bits(s), s)) * static_cast<float>(qt[c.tq][zz]);
                                         ++k;
                                     }
                                     int ox = (mx * c.h + bx) * 8, oy = (my * c.v + by) * 8;
