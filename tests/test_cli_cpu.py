@@ -223,6 +223,27 @@ def test_jpeg_decoder_matches_encoder(png_check, tmp_path, h, w, sampling, resta
     assert d.max() <= 1 and d.mean() < 1e-3
 
 
+def test_jpeg_decoder_segment_variants(png_check, tmp_path):
+    """Fill bytes before markers, a DRI segment of 0 (no restarts), no APP0 header, unknown
+    APPn segments: the same pixels as the plain file."""
+    import jpeg_encode
+    img = _test_image(20, 28, False, 5)
+    plain, expected = jpeg_encode.encode(img, sampling=(2, 2))
+    bare, _ = jpeg_encode.encode(img, sampling=(2, 2), app0=False)
+    sof = plain.index(b"\xff\xc0")
+    variants = {
+        "fill": plain[:sof] + b"\xff\xff\xff" + plain[sof:],
+        "dri0": plain[:sof] + b"\xff\xdd\x00\x04\x00\x00" + plain[sof:],
+        "app1": plain[:2] + b"\xff\xe1\x00\x08Exif\x00\x00" + plain[2:],
+        "no_app0": bare,
+    }
+    for name, data in variants.items():
+        p = tmp_path / f"{name}.jpg"
+        p.write_bytes(data)
+        got, _ = _read(png_check, p, tmp_path)
+        assert np.abs(got.astype(np.int64) - expected).max() <= 1, name
+
+
 def test_jpeg_decoder_near_lossless_against_source(png_check, tmp_path):
     """Unit quantisation tables: the decode comes back to the source image (the colour
     conversion and block order checked against the pixels, not against the writer's model)."""
