@@ -113,35 +113,6 @@ def test_trainer_densify_path(cuda):
         assert tr.sites().shape[0] == info.active_estimate
 
 
-def oracle_render_from_sites(orc, sites, w, h, passes=16, inject=4, hprobes=1, hwin=32):
-    """renderVoronoiFromSites: clear, seed, flood (ping-pong inside the field), VPT passes."""
-    n = sites.shape[0]
-    inv = 1.0 / max(w, h) ** 2
-    a0 = np.full((w * h, 4), 0xFFFFFFFF, np.uint32)
-    a1 = a0.copy()
-    a0 = orc.jfa_seed(a0, sites, w, h)
-    step = 1
-    while step < max(w, h):
-        step <<= 1
-    src, dst = a0, a1
-    s = step // 2
-    while s >= 1:
-        dst = orc.jfa_flood(src, sites, s, w, h)
-        src, dst = dst, src
-        s //= 2
-    a0, a1 = src, dst
-    packed = orc.pack_sites(sites)
-    bits = orc.hilbert_bits_for_size(w, h)
-    padded = (n + 1023) // 1024 * 1024
-    pairs = orc.radix_sort_pairs(orc.hilbert_pairs(sites, padded, w, h, bits),
-                                 0xFFFFFFFF if bits >= 16 else 1 << (2 * bits))
-    horder, hpos = orc.hilbert_order(pairs, n)
-    for i in range(passes):
-        a0, a1 = orc.vpt_pass(a0, a1, packed, n, orc.pack_jump_step(i, w, h), i >> 16, w, h, 64.0, 0,
-                              inject, horder, hpos, hprobes, hwin)
-    return orc.render(a0, a1, sites, w, h), (a0, a1)
-
-
 @pytest.mark.parametrize("w,h,n", [(128, 128, 2000), (200, 120, 5000)])
 def test_render_from_sites_matches_oracle_pipeline(cuda, orc, w, h, n):
     from sad_gb300 import _lib
@@ -155,7 +126,7 @@ def test_render_from_sites_matches_oracle_pipeline(cuda, orc, w, h, n):
     _lib.call("sad_render_from_sites", C.byref(cfg), C.c_void_p(st.data_ptr()), n, w, h,
               C.c_void_p(out.data_ptr()), C.c_void_p(scratch.data_ptr()), nbytes, None)
     torch.cuda.synchronize()
-    want, _ = oracle_render_from_sites(orc, sites, w, h)
+    want, _ = cases.oracle_render_from_sites(orc, sites, w, h)
     diff = np.abs(out.cpu().numpy() - want)
     # 16 chained candidate passes: a near-tie resolved differently can propagate, so the
     # check is on the rendered image

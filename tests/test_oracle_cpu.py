@@ -243,6 +243,37 @@ def test_jfa_then_vpt_recall(orc):
     assert hit / (w * h) > 0.98
 
 
+@pytest.mark.parametrize("w,h,n", [(96, 96, 1000), (128, 80, 3000)])
+def test_render_candidate_build_recall(orc, w, h, n):
+    """Candidate quality of the render-from-sites build (seed, JFA flood, 16 VPT passes
+    with random injection and Hilbert probes) against a brute-force top-8 over all sites,
+    by the metrics backends/metal/tests/test_jump_schedule.swift:89-136 prints (Recall@8,
+    full-list match), asserted here.  The GPU build returns the same lists
+    (test_gpu_trainer.py compares the rendered images)."""
+    from checks import packed_dist_np
+    _, sites = cases.scene(w, h, n, 21)
+    _, (c0, c1) = cases.oracle_render_from_sites(orc, sites, w, h)
+    ids = np.concatenate([c0, c1], 1).astype(np.int64)
+    inv = 1.0 / max(w, h) ** 2
+    ys, xs = np.divmod(np.arange(w * h), w)
+    every = np.arange(n)[None, :]
+    hits, full, nearest = 0, 0, 0
+    for a in range(0, w * h, 512):
+        b = min(a + 512, w * h)
+        d = packed_dist_np(sites, every, xs[a:b, None].astype(np.float64), ys[a:b, None].astype(np.float64), inv)
+        top = np.argsort(d, axis=1, kind="stable")[:, :8]
+        for k, p in enumerate(range(a, b)):
+            got = set(ids[p])
+            hit = len(set(top[k]) & got)
+            hits += hit
+            full += hit == 8
+            nearest += int(top[k, 0]) in got
+    npx = w * h
+    assert hits / (8 * npx) >= 0.999
+    assert full / npx >= 0.99
+    assert nearest / npx >= 0.999
+
+
 def test_init_gradient_weighted_accepts_textured_pixels(orc):
     w, h = 96, 64
     img, _ = cases.scene(w, h, 1, seed=2)
