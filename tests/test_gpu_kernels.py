@@ -18,7 +18,7 @@ import pytest
 import torch
 
 import cases
-from checks import assert_close_sum, assert_grads_close, assert_lists_match, packed_dist_np, raw_dist_np
+from checks import assert_grads_close, assert_lists_match, packed_dist_np, raw_dist_np
 
 pytestmark = pytest.mark.gpu
 
