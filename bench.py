@@ -170,24 +170,34 @@ def run_ours(args):
     value = ws * args.steps * iters / (total_ms / 1e3)
 
     # roofline: one instrumented fit times every fused-gradient launch with CUDA events on
-    # the trainer's stream (eager launches; the kernels are the same)
+    # the trainer's stream (eager launches; the kernels are the same), and samples the
+    # active site count every 40 iterations
     tr.enable_timing(True)
     tr.init()
-    tr.run()
+    active = []
+    for end in range(40, iters + 40, 40):
+        tr.run(min(end, iters))
+        active.append((min(end, iters) - (end - 40), tr.info().active_estimate))
     info = tr.info()
     tr.enable_timing(False)
     grad_ms = info.gpu_ms_gradients / max(1, info.gradient_launches)
     n_buf = info.site_buffer
-    # per pixel: target 12 B, candidate lists 32 B, precomputed table indices 16 B;
-    # per site: the gradient record's read-modify-write
-    alg_bytes = 60 * WIDTH * HEIGHT + 80 * n_buf
+    mean_active = sum(k * a for k, a in active) / max(1, sum(k for k, _ in active))
+    # algorithmic bytes of the fused gradient step: per pixel the target (12 B), mask (4 B)
+    # and the two candidate lists (32 B); per site the gradient read-modify-write (80 B)
+    alg_bytes = 48 * WIDTH * HEIGHT + 80 * n_buf
+    alg_active = 48 * WIDTH * HEIGHT + 80 * mean_active
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (grad_ms / 1e3) / 1e9
+    prof = profiled_kernel()
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": profiled_kernel().get("dram_bytes_per_launch"),
-                "limiter": profiled_kernel().get("limiter"),
-                "kernel": "fused_gradients_pre_kernel", "launch_ms": round(grad_ms, 5),
-                "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind}
+                "frac": round(achieved / peak, 4), "traffic": prof.get("dram_bytes_per_launch"),
+                "limiter": prof.get("limiter"),
+                "kernel": prof.get("kernel", "fused_gradients_pre_kernel"), "launch_ms": round(grad_ms, 5),
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "algorithmic_bytes_active_weighted": int(alg_active),
+                "frac_active_weighted": round(alg_active / (grad_ms / 1e3) / 1e9 / peak, 4),
+                "mean_active_sites": int(mean_active), "peak_source": peak_kind}
 
     # e2e: host image in pinned memory -> fit -> active sites + PSNR back
     host = torch.from_numpy(img).pin_memory().numpy()
@@ -225,69 +235,74 @@ def run_ours(args):
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
+        out["cpu_baseline"] = cpu_baseline()
     return out
 
 
-def cpu_fit(img, seconds: float, threads: int):
-    """Oracle fit of the workload, iterations run until `seconds` pass (>= 2)."""
+# The CPU sample, the same in the cpu_baseline leg and in --impl reference: iteration 0 of
+# the fit runs untimed (it carries the first candidate refresh), then iterations
+# 1..CPU_SAMPLE_ITERS are timed.  Until the first prune (iteration 100) all 128,000 sites are
+# active, so this is the heavy start of the fit: a conservative (low) CPU rate.
+CPU_SAMPLE_FIRST = 1
+CPU_SAMPLE_ITERS = 300
+
+
+def cpu_fit_config(threads: int):
+    """The oracle's own fit config: training_config.json read by the oracle and the bpp rule
+    applied by the oracle's solver (no product code on this path)."""
     import orc
-    from sad_gb300 import _lib
-    from sad_gb300.config import train_config
-    cfg = train_config(log_freq=0)
-    sol = _lib.BppSolution()
-    import ctypes as C
-    _lib.call("sad_solve_target_bpp", 1.0, WIDTH, HEIGHT, cfg.n_sites, cfg.max_sites, cfg.iterations,
-              1, cfg.densify_start, cfg.densify_end, cfg.densify_freq, cfg.densify_percentile,
-              cfg.prune_during_densify, cfg.prune_start, cfg.prune_end, cfg.prune_freq,
-              cfg.prune_percentile, 65536, C.byref(sol))
-    cfg.prune_percentile, cfg.densify_percentile = sol.prune_percentile, sol.densify_percentile
-    f = orc.Fit(orc.fit_config_from(cfg, threads=threads), img)
-    t0 = time.perf_counter()
-    it = 0
-    while it < 2 or time.perf_counter() - t0 < seconds:
-        f.run(it, it + 1)
-        it += 1
-    dt = time.perf_counter() - t0
-    f.close()
-    return it, dt
+    cfg_path = os.path.join(ROOT, "sad_gb300", "training_config.json")
+    return orc.fit_config_json(cfg_path, WIDTH, HEIGHT, target_bpp=1.0, threads=threads)
 
 
-def cpu_baseline(seconds: float = 15.0):
-    from sad_gb300.synthetic import synthetic_image
+def cpu_chunks(total: int, parts: int) -> list[int]:
+    parts = max(1, parts)
+    total = max(total, parts)
+    return [total // parts + (1 if i < total % parts else 0) for i in range(parts)]
+
+
+def cpu_sample_text(its: int, secs: float, threads: int) -> str:
+    return (f"iterations {CPU_SAMPLE_FIRST}-{CPU_SAMPLE_FIRST + its - 1} of the same 1024x1024 fit "
+            f"after an untimed iteration 0 ({secs:.1f} s, OpenMP x{threads})")
+
+
+def cpu_baseline():
+    import orc
+    from sad_gb300.synthetic import synthetic_image  # numpy generator, no native code
     threads = os.cpu_count() or 1
+    orc.set_threads(threads)
     img = synthetic_image(WIDTH, HEIGHT, seed=0)
-    it, dt = cpu_fit(img, seconds, threads)
-    return {"value": round(it / dt, 4), "unit": "iters/s", "cores": threads, "kind": "port",
-            "sample": f"first {it} iterations of the same 1024x1024 fit ({dt:.1f} s, OpenMP x{threads})"}
+    secs = sum(orc.timed_fit_sample(cpu_fit_config(threads), img, CPU_SAMPLE_FIRST, [CPU_SAMPLE_ITERS]))
+    return {"value": round(CPU_SAMPLE_ITERS / secs, 4), "unit": "iters/s", "cores": threads, "kind": "port",
+            "sample": cpu_sample_text(CPU_SAMPLE_ITERS, secs, threads)}
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return None
-    from sad_gb300.synthetic import synthetic_image
     import orc
+    from sad_gb300.synthetic import synthetic_image  # numpy generator, no native code
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
     img = synthetic_image(WIDTH, HEIGHT, seed=0)
-    per_step = max(1.0, args.cpu_seconds / max(1, args.steps + args.warmup))
-    for _ in range(args.warmup):
-        cpu_fit(img, per_step / 4, threads)
-    its, secs = 0, 0.0
-    for _ in range(args.steps):
-        it, dt = cpu_fit(img, per_step, threads)
-        its += it
-        secs += dt
+    cfg = cpu_fit_config(threads)
+    chunks = cpu_chunks(CPU_SAMPLE_ITERS, args.steps)
+    if args.warmup > 0:  # warm-up steps on a separate fit, so the timed window is the same
+        orc.timed_fit_sample(cfg, img, CPU_SAMPLE_FIRST, [chunks[0]] * args.warmup)
+    times = orc.timed_fit_sample(cfg, img, CPU_SAMPLE_FIRST, chunks)
+    its, secs = sum(chunks), sum(times)
     value = its / secs
     return {"metric": METRIC, "value": round(value, 4), "unit": "iters/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / args.steps, 2),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * secs / len(times), 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": DATA, "impl": "reference",
             "config": {"workload": WORKLOAD, "image": f"{WIDTH}x{HEIGHT}",
-                       "step": "a bounded sample (time-limited run of the fit's first iterations)"},
+                       "step": f"a bounded sample: iterations {CPU_SAMPLE_FIRST}-{CPU_SAMPLE_FIRST + its - 1} "
+                               f"of the fit in {len(times)} timed chunks",
+                       "l2": "host cores; no device involved"},
             "cpu_baseline": {"value": round(value, 4), "unit": "iters/s", "cores": threads, "kind": "port",
-                             "sample": f"{its} iterations over {args.steps} steps, OpenMP x{threads}"},
+                             "sample": cpu_sample_text(its, secs, threads)},
             "e2e": {"value": round(value, 4), "unit": "iters/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "note": "the reference's path is CUDA-only; this is the CPU restatement of its kernels"}
@@ -509,7 +524,6 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     ap.add_argument("--profile-iters", type=int, default=200)

@@ -153,7 +153,8 @@ sad_status_t sad_compute_gradients_tiled(
  * point (value * 2^24, bitwise reproducible).  fix12_out is a zero-initialised device
  * [site_count][12] int64 buffer receiving the sums: slots 0-9 the gradients in the order
  * of sad_compute_gradients_tiled's arrays; with compute_removal, slot 10 the removal delta
- * times *removal_scale_out (a power of two <= 1 chosen for the image size) and slot 11 the
+ * times *removal_scale_out (a power of two, which may exceed 1, chosen for the image size
+ * so that the sums fit in int64) and slot 11 the
  * number of pixels whose delta is the 1e6 sentinel (excluded from slot 10).
  * scratch: sad_compute_gradients_fixed_scratch_bytes(site_count, width, height) bytes.
  * replaces: launchComputeGradientsTiled, backends/cuda/src/gradients.cu:491-531, as
@@ -226,8 +227,9 @@ sad_status_t sad_radix_sort_pairs(uint32_t* pairs, uint32_t count, uint32_t max_
  * are rejected (SAD_ERR_INVALID_ARGUMENT).  It serves hosts that must not allocate device
  * memory on their call path: one with a fixed, pre-reserved memory budget, or a
  * latency-bound loop in which an allocation call (which can synchronise the device) is
- * not acceptable.  The first call on a device looks the array up (with that device
- * current) and should come before any stream capture.  Nothing in the scratch needs to
+ * not acceptable.  Each call looks the array's address up on the current device (a host
+ * lookup); the first call on a device may load the module and should come before any
+ * stream capture.  Nothing in the scratch needs to
  * start at zero.  Overlapping calls on one device (other streams or host threads) share
  * the scratch and race: the caller must serialise them.
  * No counterpart in the reference (its sort always takes caller-allocated scratch). */

@@ -391,6 +391,72 @@ def fit_config_from(train_cfg, threads=0) -> FitConfig:
     return c
 
 
+# training_config.json keys -> FitConfig fields, with the reference's defaults for keys a
+# file leaves out (backends/cuda/src/sad_cuda.cu:422-517, loadDefaults; densify is on by
+# default, sad_cuda.cu:609).  The learning-rate keys are the reference's *_BASE rates.
+_JSON_KEYS = {
+    "DEFAULT_SITES": ("n_sites", int, 128000), "DEFAULT_MAX_SITES": ("max_sites", int, 128000),
+    "DEFAULT_ITERS": ("iterations", int, 4000), "PRUNE_PERCENTILE": ("prune_pct", float, 0.033),
+    "PRUNE_DURING_DENSIFY": ("prune_during_densify", bool, True), "PRUNE_START": ("prune_start", int, 100),
+    "PRUNE_FREQ": ("prune_freq", int, 40), "PRUNE_END": ("prune_end", int, 3000),
+    "DENSIFY_START": ("densify_start", int, 20), "DENSIFY_FREQ": ("densify_freq", int, 20),
+    "DENSIFY_END": ("densify_end", int, 3000), "DENSIFY_PERCENTILE": ("densify_pct", float, 0.01),
+    "DENSIFY_SCORE_ALPHA": ("densify_alpha", float, 0.7), "CAND_UPDATE_FREQ": ("cand_freq", int, 8),
+    "CAND_UPDATE_PASSES": ("cand_passes", int, 1), "CAND_RADIUS_SCALE": ("cand_radius_scale", float, 64.0),
+    "CAND_RADIUS_PROBES": ("cand_radius_probes", int, 0), "CAND_INJECT_COUNT": ("cand_inject", int, 4),
+    "CAND_HILBERT_WINDOW": ("hilbert_window", int, 32), "CAND_HILBERT_PROBES": ("hilbert_probes", int, 1),
+    "LR_POS_BASE": ("lr_pos", float, 0.025), "LR_TAU_BASE": ("lr_tau", float, 0.01),
+    "LR_RADIUS_BASE": ("lr_radius", float, 0.01), "LR_COLOR_BASE": ("lr_color", float, 0.01),
+    "LR_DIR_BASE": ("lr_dir", float, 0.0025), "LR_ANISO_BASE": ("lr_aniso", float, 0.025),
+    "INIT_LOG_TAU": ("init_log_tau", float, 5.0), "INIT_RADIUS": ("init_radius", float, 4.0),
+    "BETA1": ("beta1", float, 0.9), "BETA2": ("beta2", float, 0.999), "EPS": ("eps", float, 1e-8),
+}
+
+
+def fit_config_json(path: str, w: int, h: int, target_bpp: float | None = 1.0, threads: int = 0,
+                    **overrides) -> FitConfig:
+    """Oracle fit config read straight from a training_config.json (no product code
+    involved), with the bpp rule applied when target_bpp > 0: the densify / prune
+    percentiles are scaled as solveTargetBpp does (backends/cuda/src/sad_cuda.cu:904-1066,
+    max split 65536 per event, sad_cuda.cu:1095)."""
+    import json
+    with open(path) as f:
+        data = json.load(f)
+    c = FitConfig()
+    c.densify = 1
+    for key, (field, typ, default) in _JSON_KEYS.items():
+        v = data.get(key, default)
+        setattr(c, field, int(bool(v)) if typ is bool else typ(v))
+    for field, v in overrides.items():
+        setattr(c, field, v)
+    if target_bpp and target_bpp > 0:
+        sol = solve_target_bpp(float(target_bpp), int(w), int(h), c.n_sites, c.max_sites, c.iterations,
+                               c.densify, c.densify_start, c.densify_end, c.densify_freq, c.densify_pct,
+                               c.prune_during_densify, c.prune_start, c.prune_end, c.prune_freq,
+                               c.prune_pct, 65536)
+        c.densify_pct, c.prune_pct = float(sol[0]), float(sol[1])
+    c.threads = int(threads)
+    return c
+
+
+def timed_fit_sample(cfg: FitConfig, target: np.ndarray, first: int, chunks: list[int]):
+    """Bounded CPU sample of one fit: iterations [0, first) run untimed (setup), then each
+    chunk of consecutive iterations is timed on its own.  Returns the per-chunk seconds."""
+    import time
+    f = Fit(cfg, target)
+    try:
+        f.run(0, first)
+        it, out = first, []
+        for k in chunks:
+            t0 = time.perf_counter()
+            f.run(it, it + k)
+            out.append(time.perf_counter() - t0)
+            it += k
+        return out
+    finally:
+        f.close()
+
+
 def pack_inference_sites(sites, w, h):
     """16-byte quantised sites: (packed [N,4] u32, quant [10] f32)."""
     sites = _c(sites, np.float32)

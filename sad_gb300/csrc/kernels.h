@@ -90,7 +90,7 @@ struct GradParams {
     float* soa[10];
     float* removal;
     long long* fix12;
-    float removal_fix_mul;  // fixed-point path: removal delta pre-scale (power of two <= 1)
+    float removal_fix_mul;  // fixed-point path: removal delta pre-scale (a power of two, may exceed 1)
     int compute_removal;
     // trainer: the candidate field's tile registration, computed once per field refresh
     // (nullptr: register keys inside the gradient kernel)

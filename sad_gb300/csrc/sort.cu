@@ -16,8 +16,6 @@
 #include "host_common.h"
 #include "kernels.h"
 
-#include <mutex>
-
 namespace sad {
 
 constexpr int kSortThreads = 256;
@@ -186,12 +184,14 @@ extern "C" sad_status_t sad_radix_sort_pairs(uint32_t* pairs, uint32_t count,
 
 // ---------------------------------------------------------------------------
 // Allocation-free entry point: the sort's scratch is a fixed file-scope device array,
-// sized for SAD_NOALLOC_SORT_MAX_PAIRS pairs.  Its address is fetched once per device
-// with cudaGetSymbolAddress (the first call on a device does it, with that device
-// current); host code never uses the symbol itself as a device address.  Nothing in the
-// scratch has to start at zero: each pass writes the histograms and the ping-pong buffer
-// before reading them.  The scratch is shared: calls that overlap on one device (other
-// streams or host threads) race on it and must be serialised by the caller.
+// sized for SAD_NOALLOC_SORT_MAX_PAIRS pairs.  Every call looks its address up with
+// cudaGetSymbolAddress on the current device (a host-side lookup, so a context that was
+// torn down and re-created never leaves a stale address behind); host code never uses the
+// symbol itself as a device address.  The first call on a device may load the module, so
+// it should come before any stream capture.  Nothing in the scratch has to start at zero:
+// each pass writes the histograms and the ping-pong buffer before reading them.  The
+// scratch is shared: calls that overlap on one device (other streams or host threads) race
+// on it and must be serialised by the caller.
 // ---------------------------------------------------------------------------
 namespace sad {
 
@@ -203,22 +203,11 @@ constexpr size_t kNoAllocScratchBytes =
 
 static __device__ __align__(256) unsigned char g_noalloc_sort_scratch[kNoAllocScratchBytes];
 
-static std::mutex g_noalloc_mutex;
-static void* g_noalloc_scratch[64];
-
 static sad_status_t noalloc_scratch(void** out) {
-    int dev = 0;
-    SAD_TRY(check_cuda(cudaGetDevice(&dev), "sad_radix_sort_pairs_noalloc: cudaGetDevice"));
-    if (dev < 0 || dev >= 64)
-        return fail(SAD_ERR_UNSUPPORTED, "sad_radix_sort_pairs_noalloc: device ordinal out of range (>= 64)");
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_scratch[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sort_scratch);
-        if (e != cudaSuccess) return check_cuda(e, "sad_radix_sort_pairs_noalloc: cudaGetSymbolAddress");
-        g_noalloc_scratch[dev] = p;
-    }
-    *out = g_noalloc_scratch[dev];
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_sort_scratch);
+    if (e != cudaSuccess) return check_cuda(e, "sad_radix_sort_pairs_noalloc: cudaGetSymbolAddress");
+    *out = p;
     return SAD_OK;
 }
 

@@ -2,7 +2,7 @@
 
     oracle/ref/stage.sh /path/to/reference     # copy its sources to baseline/_ref/ (git-ignored)
     oracle/ref/build.sh                        # nvcc -> oracle/_ref/ref_harness (needs a GPU to run)
-    python tests/golden/make_fixtures.py [outdir]
+    python tests/golden/make_fixtures.py [outdir] [--only=chains]
 
 Each case writes seeded inputs to a scratch directory, runs one reference kernel through
 oracle/_ref/ref_harness, and stores inputs + the reference's outputs in <outdir>/<case>.npz
@@ -242,5 +242,83 @@ def main(outdir: str):
          split_sites=split_sites, split_adam=split_adam, params=np.array([n, pc, w, h, ns, cap, k], np.int64))
 
 
+def chains(outdir: str):
+    """Chains of candidate passes through the reference, recorded pass by pass
+    (cand_chain.npz): the render-from-sites build of renderVoronoiFromSites
+    (backends/cuda/src/sad_cuda.cu:1616-1655, 1774-1812) -- JFA flood passes from the
+    seeded field down to step 1 (ping-ponging as runJFA does, so the first VPT pass sees
+    an intermediate field in slots 4-7), then 16 VPT passes with Hilbert probes, 4
+    injections and the render -- on a 200x152
+    image with 3000 sites.  The seed comes from the oracle (lowest id per texel; the
+    reference's seed store is a race), and so do the packed sites and Hilbert order, which
+    have fixtures of their own.  Each pass's output is recorded as a SHA-256 digest (the
+    final JFA and VPT fields in full), so a difference is located at the first pass it
+    appears in."""
+    import hashlib
+
+    def digest(*a):
+        return np.frombuffer(hashlib.sha256(b"".join(np.ascontiguousarray(x).tobytes() for x in a)).digest(),
+                             np.uint8)
+    import orc
+    tmp = tempfile.mkdtemp()
+    w, h, n = 200, 152, 3000
+    img, sites = cases.scene(w, h, n, 60)
+    sites[::13, 0] = -1
+    inv = f32s(1.0 / max(w, h) ** 2)
+    field = orc.jfa_seed(np.full((w * h, 4), U32, np.uint32), sites, w, h)
+    arrays = dict(sites=sites, seed=field.copy(), params=np.array([w, h, n], np.int64),
+                  inv_s2=np.float32(inv))
+    step = 1
+    while step < max(w, h):
+        step <<= 1
+    steps, fields = [], [field]
+    s_ = step // 2
+    while s_ >= 1:
+        put(tmp, "cand0", field)
+        put(tmp, "sites", sites)
+        run("jfa_flood", tmp, n, s_, inv, w, h, 1, w, h)
+        field = get(tmp, "out", np.uint32, (w * h, 4))
+        arrays[f"jfa_{s_}"] = digest(field)
+        fields.append(field)
+        steps.append(s_)
+        s_ //= 2
+    arrays["jfa_steps"] = np.array(steps, np.int64)
+    arrays["jfa_final"] = field.copy()
+    packed = orc.pack_sites(sites)
+    bits = orc.hilbert_bits_for_size(w, h)
+    padded = (n + 1023) // 1024 * 1024
+    pairs = orc.radix_sort_pairs(orc.hilbert_pairs(sites, padded, w, h, bits),
+                                 0xFFFFFFFF if bits >= 16 else 1 << (2 * bits))
+    horder, hpos = orc.hilbert_order(pairs, n)
+    arrays.update(packed=packed, horder=horder, hpos=hpos)
+    # runJFA's ping-pong (sad_cuda.cu:1641-1654): after an even number of passes slots 4-7
+    # hold the second-last pass's lists; after an odd number both halves hold the last
+    c0 = field
+    c1 = fields[-2] if len(steps) % 2 == 0 else field
+    for i in range(16):
+        st = orc.pack_jump_step(i, w, h)
+        for k, v in (("cand0", c0), ("cand1", c1), ("packed", packed), ("horder", horder), ("hpos", hpos)):
+            put(tmp, k, v)
+        run("vpt", tmp, n, st, inv, i >> 16, 64.0, 0, 4, 1, 32, 1, w, h, w, h)
+        c0 = get(tmp, "out0", np.uint32, (w * h, 4))
+        c1 = get(tmp, "out1", np.uint32, (w * h, 4))
+        arrays[f"vpt_{i}"] = digest(c0, c1)
+    arrays["vpt_final0"], arrays["vpt_final1"] = c0.copy(), c1.copy()
+    put(tmp, "cand0", c0)
+    put(tmp, "cand1", c1)
+    put(tmp, "sites", sites)
+    run("render", tmp, n, w, h, w, h, inv)
+    arrays["render"] = get(tmp, "out", np.float32, (h, w, 3))
+    np.savez_compressed(os.path.join(outdir, "cand_chain.npz"), **arrays)
+    print("wrote cand_chain")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else HERE)
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    out = args[0] if args else HERE
+    if "--only=chains" in sys.argv:  # the pass-by-pass chains alone
+        os.makedirs(out, exist_ok=True)
+        chains(out)
+    else:
+        main(out)
+        chains(out)

@@ -9,9 +9,14 @@ called through the C ABI, to the same outputs.  Tolerances:
   * JFA seed: bit-exact where one site maps to a texel; where several collide, the
     reference keeps whichever write lands last (a race), this library the lowest id --
     the reference's pick must be one of the colliding sites;
-  * JFA flood and VPT candidate lists: oracle bit-exact; GPU identical except where two
-    distances agree to 1e-5 relative, on >= 99% of pixels;
+  * JFA flood and VPT candidate lists: bit-exact, oracle and GPU (the GPU kernels use the
+    reference's FP32 operations in its order; also over chains of passes, below);
   * rendered RGB: oracle <= 2e-6, GPU <= 1e-5 max abs (FMA contraction);
+  * autograd adjoint (the reference's render_sad_backward): every entry within 1e-3
+    (oracle) / 1e-4 (GPU) of its sum A of absolute pixel terms, and each parameter's
+    vector within a relative L2 error of 1e-4; the scale is A, not the entry itself,
+    because the reference sums float terms with atomics in no fixed order and entries
+    whose terms cancel have no relative accuracy to hold;
   * per-site gradients: relative L2 error per parameter <= 1e-4 (oracle) / 1e-3 (GPU),
     every entry within 1% / 5% of its sum of absolute pixel terms (the reference sums
     with float atomics in no fixed order);
@@ -25,7 +30,7 @@ import os
 import numpy as np
 import pytest
 
-from checks import assert_grads_close, assert_lists_match, packed_dist_np, raw_dist_np
+from checks import assert_close_sum, assert_grads_close
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 U32 = 0xFFFFFFFF
@@ -132,6 +137,42 @@ def test_oracle_gradients(orc, name):
         assert np.all(np.abs(z["removal"] - r) <= 1e-3 * np.maximum(np.abs(r), 1.0))
 
 
+ADJ_CASES = ["knn_64x48", "random_61x37", "knn_97x65"]
+
+
+def adjoint_case(name):
+    z = load("render_backward")
+    w, h, n = (int(v) for v in z[f"{name}_params"])
+    return ({k: z[f"{name}_{k}"] for k in ("cand0", "cand1", "sites", "grad_out", "grad_sites", "render")},
+            w, h, n, float(z[f"{name}_inv_s2"]))
+
+
+def check_adjoint(got, want, absw, rtol):
+    """[N,10] gradients against the reference's: each parameter's vector within 1e-4
+    relative L2, every entry within rtol of its absolute-term sum."""
+    for k in range(10):
+        num = np.linalg.norm(got[:, k] - want[:, k])
+        assert num <= 1e-4 * max(np.linalg.norm(want[:, k]), 1e-12), (k, num)
+    assert_close_sum(got, want, absw, rtol=rtol, atol=1e-7, what="adjoint")
+
+
+@pytest.mark.parametrize("name", ADJ_CASES)
+def test_oracle_render_backward(orc, name):
+    z, w, h, n, inv = adjoint_case(name)
+    r = orc.render(z["cand0"], z["cand1"], z["sites"], w, h, inv_s2=inv)
+    assert np.max(np.abs(r - z["render"])) <= 2e-6
+    g, a = orc.render_backward(z["cand0"], z["cand1"], z["sites"], z["grad_out"], w, h, inv_s2=inv)
+    check_adjoint(g, z["grad_sites"].astype(np.float64), a, rtol=1e-3)
+    if not name.startswith("knn"):
+        return
+    # the reference against the FP64 restatement of the same adjoint, on the nearest-site
+    # fields a fit sees (a random field's far candidates make single FP32 terms
+    # ill-conditioned, in the reference as in any FP32 evaluation)
+    g64 = orc.render_backward_d(z["cand0"], z["cand1"], z["sites"].astype(np.float64),
+                                z["grad_out"].astype(np.float64), w, h, inv)
+    assert_close_sum(z["grad_sites"].astype(np.float64), g64, a, rtol=2e-4, atol=1e-7, what="reference vs FP64")
+
+
 def test_oracle_tau_diffuse(orc):
     z = load("tau")
     w, h, n = (int(v) for v in z["params"])
@@ -182,6 +223,51 @@ def check_split(ss, sa, z):
     np.testing.assert_allclose(ss[:, rest], z["split_sites"][:, rest], rtol=1e-4, atol=2e-4)
     np.testing.assert_allclose(ss[:, ang], z["split_sites"][:, ang], rtol=1e-2, atol=1e-2)
     np.testing.assert_array_equal(sa, z["split_adam"])
+
+
+def sha(*arrays):
+    import hashlib
+    return np.frombuffer(hashlib.sha256(b"".join(np.ascontiguousarray(a).tobytes() for a in arrays)).digest(),
+                         np.uint8)
+
+
+def chain_start(z, floods):
+    """(cand0, cand1) entering the first VPT pass: runJFA's ping-pong of the flood
+    outputs (sad_cuda.cu:1641-1654).  floods[0] is the seeded field, then one entry per
+    flood pass."""
+    if (len(floods) - 1) % 2 == 0:
+        return floods[-1], floods[-2]
+    return floods[-1], floods[-1]
+
+
+def check_chain(z, flood_fn, vpt_fn):
+    """Run the chain with the given pass functions and compare every pass's digest."""
+    w, h, n = (int(v) for v in z["params"])
+    field, floods = z["seed"], [z["seed"]]
+    for s_ in z["jfa_steps"]:
+        field = flood_fn(field, int(s_))
+        np.testing.assert_array_equal(sha(field), z[f"jfa_{int(s_)}"], err_msg=f"JFA flood step {int(s_)}")
+        floods.append(field)
+    np.testing.assert_array_equal(field, z["jfa_final"])
+    c0, c1 = chain_start(z, floods)
+    for i in range(16):
+        c0, c1 = vpt_fn(c0, c1, i)
+        np.testing.assert_array_equal(sha(c0, c1), z[f"vpt_{i}"], err_msg=f"VPT pass {i}")
+    np.testing.assert_array_equal(c0, z["vpt_final0"])
+    np.testing.assert_array_equal(c1, z["vpt_final1"])
+    return c0, c1
+
+
+def test_oracle_candidate_chain(orc):
+    z = load("cand_chain")
+    w, h, n = (int(v) for v in z["params"])
+    inv = float(z["inv_s2"])
+    np.testing.assert_array_equal(orc.pack_sites(z["sites"]), z["packed"])
+    c0, c1 = check_chain(
+        z, lambda f, s_: orc.jfa_flood(f, z["sites"], s_, w, h, 1, None, None, inv),
+        lambda a, b, i: orc.vpt_pass(a, b, z["packed"], n, orc.pack_jump_step(i, w, h), i >> 16, w, h, 64.0, 0, 4,
+                                     z["horder"], z["hpos"], 1, 32))
+    assert np.max(np.abs(orc.render(c0, c1, z["sites"], w, h, inv_s2=inv) - z["render"])) <= 2e-6
 
 
 # ---------------------------------------------------------------------------
@@ -257,11 +343,10 @@ def test_gpu_jfa_flood(gops):
     z = load("jfa_flood")
     n, w, h = (int(v) for v in z["params"])
     inv = float(z["inv_s2"])
-    dist = lambda ids, xs, ys: raw_dist_np(z["sites"], ids, xs, ys, inv)
     for step in (32, 4, 1):
         out = torch.empty((w * h, 4), dtype=torch.int32, device="cuda")
         got = u32(gops.jfa_flood(t32(z[f"in_{step}"]), out, tf(z["sites"]), inv, 0, step, 1, w, h))
-        assert_lists_match(got, z[f"out_{step}"], dist, w, h)
+        np.testing.assert_array_equal(got, z[f"out_{step}"])
 
 
 @pytest.mark.gpu
@@ -282,9 +367,54 @@ def test_gpu_vpt(gops, orc, name):
         gops.update_candidates_compact(t32(z["cand0"]), t32(z["cand1"]), o0, o1, packed, ho, hp, inv, n,
                                        step, idx >> 16, 64.0, 0, 4, 1 if hil else 0, 32 if hil else 0, 1,
                                        w, h, w, h)
-        got = np.concatenate([u32(o0), u32(o1)], axis=1)
-        want = np.concatenate([z[f"out0_{idx}"], z[f"out1_{idx}"]], axis=1)
-        assert_lists_match(got, want, lambda ids, xs, ys: packed_dist_np(z["sites"], ids, xs, ys, inv), w, h)
+        np.testing.assert_array_equal(u32(o0), z[f"out0_{idx}"])
+        np.testing.assert_array_equal(u32(o1), z[f"out1_{idx}"])
+
+
+@pytest.mark.gpu
+def test_gpu_candidate_chain(gops):
+    """Eight JFA flood passes and sixteen VPT passes chained through this library's
+    kernels, bit-exact against the reference pass by pass; then the whole render-from-sites
+    path (sad_render_from_sites: its own seed, flood and VPT kernels on prepared site
+    records, and the render) against the reference's render of the same chain."""
+    import ctypes as C
+    torch = _t()
+    from sad_gb300 import _lib
+    z = load("cand_chain")
+    w, h, n = (int(v) for v in z["params"])
+    inv = float(z["inv_s2"])
+    s_t = tf(z["sites"])
+    packed = torch.from_numpy(z["packed"].view(np.float16)).cuda()
+    ho, hp = t32(z["horder"]), t32(z["hpos"])
+
+    def flood(f, s_):
+        out = torch.empty((w * h, 4), dtype=torch.int32, device="cuda")
+        return u32(gops.jfa_flood(t32(f), out, s_t, inv, 0, s_, 1, w, h))
+
+    def vpt(a, b, i):
+        o0 = torch.empty((w * h, 4), dtype=torch.int32, device="cuda")
+        o1 = torch.empty((w * h, 4), dtype=torch.int32, device="cuda")
+        gops.update_candidates_compact(t32(a), t32(b), o0, o1, packed, ho, hp, inv, n,
+                                       int(np.uint32(_lib.load().sad_pack_jump_step(i, w, h))), i >> 16,
+                                       64.0, 0, 4, 1, 32, 1, w, h, w, h)
+        return u32(o0), u32(o1)
+
+    seeded = u32(gops.jfa_seed(t32(np.full((w * h, 4), U32, np.uint32)), s_t, 0, 1, w, h))
+    np.testing.assert_array_equal(seeded, z["seed"])
+    check_chain(z, flood, vpt)
+
+    lib = _lib.load()
+    cfg = _lib.RenderConfig()
+    lib.sad_render_config_default(C.byref(cfg))
+    assert (cfg.candidate_passes, cfg.use_jfa, cfg.jfa_rounds, cfg.cand_inject_count, cfg.cand_hilbert_probes,
+            cfg.cand_hilbert_window, cfg.cand_radius_probes) == (16, 1, 1, 4, 1, 32, 0)
+    nb = lib.sad_render_scratch_bytes(n, w, h, 1)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    out = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
+    assert lib.sad_render_from_sites(C.byref(cfg), C.c_void_p(s_t.data_ptr()), n, w, h, C.c_void_p(out.data_ptr()),
+                                     C.c_void_p(scratch.data_ptr()), nb, None) == 0, lib.sad_last_error()
+    torch.cuda.synchronize()
+    assert np.max(np.abs(out.cpu().numpy() - z["render"])) <= 1e-5
 
 
 @pytest.mark.gpu
@@ -303,6 +433,20 @@ def test_gpu_gradients(gops, orc, name):
     if rem:
         r = bufs[10].cpu().numpy()
         assert np.all(np.abs(r - z["removal"]) <= 1e-3 * np.maximum(np.abs(z["removal"]), 1.0))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ADJ_CASES)
+def test_gpu_render_backward(gops, orc, name):
+    """torch.ops.sad.render_sad_backward (this library's adjoint kernel) against the
+    reference's render_sad_backward on the same inputs."""
+    z, w, h, n, inv = adjoint_case(name)
+    got = gops.render_sad_backward(t32(z["cand0"]), t32(z["cand1"]), tf(z["sites"]), tf(z["grad_out"]),
+                                   inv, w, h).cpu().numpy().astype(np.float64)
+    _, a = orc.render_backward(z["cand0"], z["cand1"], z["sites"], z["grad_out"], w, h, inv_s2=inv)
+    check_adjoint(got, z["grad_sites"].astype(np.float64), a, rtol=1e-4)
+    img = gops.render_sad(t32(z["cand0"]), t32(z["cand1"]), tf(z["sites"]), inv, w, h).cpu().numpy()
+    assert np.max(np.abs(img - z["render"])) <= 1e-5
 
 
 @pytest.mark.gpu

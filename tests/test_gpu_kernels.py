@@ -288,6 +288,8 @@ def test_trainer_gradients_match_oracle(ops, orc, w, h, n, field, removal, maske
     fix, scale = _fixed_gradients(w, h, n, c0, c1, img, rendered, mask, sites, removal, ssim)
     again, _ = _fixed_gradients(w, h, n, c0, c1, img, rendered, mask, sites, removal, ssim)
     np.testing.assert_array_equal(fix, again)
+    m, e = np.frexp(scale)  # the removal pre-scale is a power of two (it may exceed 1)
+    assert scale > 0 and m == 0.5, scale
     got = fix[:, :10].T.astype(np.float64) / 2.0 ** 24
     g, a, rem = orc.compute_gradients(c0, c1, img, sites, w, h, mask=mask if masked else None,
                                       rendered=rendered, ssim_weight=ssim, removal=removal)

@@ -70,3 +70,28 @@ def test_noalloc_sort_rejects_oversize_and_handles_trivial(lib):
     assert lib.sad_radix_sort_pairs_noalloc(None, 0, 100, None) == 0
     torch.cuda.synchronize()
     assert one.tolist() == [[7, 3]]
+
+
+def test_noalloc_sort_on_a_side_stream_after_the_default_stream(lib):
+    """The documented serialised use across streams: a call on the default stream, then,
+    ordered after it by an event, a call on another stream; both results must equal the
+    scratch-taking entry point's."""
+    a = _pairs(150001, 0xFFFFFFFF, 11)
+    b = _pairs(70001, 65536, 12)
+    want_a = _sort_with_scratch(lib, a, 0xFFFFFFFF)
+    want_b = _sort_with_scratch(lib, b, 65536)
+    torch.cuda.synchronize()
+    got_a = a.clone()
+    got_b = b.clone()
+    side = torch.cuda.Stream()
+    done = torch.cuda.Event()
+    st = lib.sad_radix_sort_pairs_noalloc(_ptr(got_a), a.shape[0], 0xFFFFFFFF, None)
+    assert st == 0, lib.sad_last_error().decode()
+    done.record(torch.cuda.default_stream())
+    side.wait_event(done)
+    st = lib.sad_radix_sort_pairs_noalloc(_ptr(got_b), b.shape[0], 65536, C.c_void_p(side.cuda_stream))
+    assert st == 0, lib.sad_last_error().decode()
+    side.synchronize()
+    torch.cuda.synchronize()
+    assert torch.equal(got_a, want_a)
+    assert torch.equal(got_b, want_b)
