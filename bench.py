@@ -503,12 +503,18 @@ def serve_sweep(args, rates, workers, budget, fit_cfg, fit_imgs, max_fits):
 
 def run_profile(args):
     """Eager (graph-free) fit of the workload for `--profile-iters` iterations, so every
-    kernel is a separate launch for ncu; nothing is timed."""
+    kernel is a separate launch for ncu; nothing is timed.  --profile-sites N fits N sites
+    with neither pruning nor densification instead: the site density of a later phase of
+    the same fit (8192: its last quarter) in a short run."""
     import torch
     from sad_gb300.synthetic import synthetic_image
     from sad_gb300.trainer import Trainer
     img = synthetic_image(WIDTH, HEIGHT, seed=0)
-    tr = Trainer(WIDTH, HEIGHT, log_freq=0, use_graphs=0)
+    extra = {}
+    if args.profile_sites > 0:
+        extra = dict(n_sites=args.profile_sites, max_sites=args.profile_sites, target_bpp=0.0,
+                     prune_percentile=0.0, densify=0)
+    tr = Trainer(WIDTH, HEIGHT, log_freq=0, use_graphs=0, **extra)
     tr.set_target(torch.from_numpy(img).cuda())
     tr.init()
     tr.run(args.profile_iters)
@@ -527,6 +533,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     ap.add_argument("--profile-iters", type=int, default=200)
+    ap.add_argument("--profile-sites", type=int, default=0)
     ap.add_argument("--workload", default="fit", choices=["fit", "batch", "serve"],
                     help="fit: the 1024x1024 headline fit; batch: 64 mixed-size fits through the "
                          "executor; serve: the Poisson render/fit mix")

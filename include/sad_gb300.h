@@ -247,6 +247,17 @@ sad_status_t sad_write_split_indices(const uint32_t* pairs, uint32_t* indices, u
 sad_status_t sad_prune_sites(float* sites, const uint32_t* indices, uint32_t count,
                              sad_stream_t stream);
 
+/* Stream compaction of the active sites: alive_out[0..k) = the ascending indices i <
+ * site_count whose pos_x >= 0, and *count_dev = k (a device word, written on the stream).
+ * scratch: sad_compact_active_scratch_bytes(site_count) bytes.  The trainer runs the same
+ * kernels after every prune, so its per-site kernels walk only the active sites.
+ * replaces: filterActiveSites, backends/cuda/src/sad_cuda.cu:1657-1666 (the reference
+ * compacts only on the host, at export) */
+size_t sad_compact_active_scratch_bytes(uint32_t site_count);
+sad_status_t sad_compact_active(const float* sites, uint32_t site_count, uint32_t* alive_out,
+                                uint32_t* count_dev, void* scratch, size_t scratch_bytes,
+                                sad_stream_t stream);
+
 /* Split parents along the error-covariance principal axis (or the image gradient); the
  * second child goes to current_site_count + i; both Adam states are reset.
  * replaces: launchSplitSites, backends/cuda/src/densify_prune.cu:335-357 */

@@ -98,6 +98,8 @@ SIGNATURES = {
     "sad_radix_sort_pairs_noalloc": (st, [vp, u32, u32, vp]),
     "sad_write_split_indices": (st, [vp, vp, u32, vp]),
     "sad_prune_sites": (st, [vp, vp, u32, vp]),
+    "sad_compact_active_scratch_bytes": (sz, [u32]),
+    "sad_compact_active": (st, [vp, u32, vp, vp, vp, sz, vp]),
     "sad_split_sites": (st, [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp, vp, u32, vp, i32, i32, vp]),
     "sad_compute_site_stats": (st, [vp, vp, vp, vp, vp, f32, u32] + [vp] * 8 + [i32] * 4 + [vp]),
     "sad_init_temp_bytes": (sz, [u32]),

@@ -62,11 +62,29 @@ __device__ __forceinline__ SiteGeom geom_from_packed(uint4 v) {
 
 // Trainer form: the same record built once per site per refresh (32-byte gathers in the
 // pass instead of 16-byte gathers plus two expf and a division per visit).
+__device__ __forceinline__ void pack_geom_one(const Site* __restrict__ sites, SiteGeom* __restrict__ out,
+                                              uint32_t i);
+
 __global__ void pack_geom_kernel(const Site* __restrict__ sites, SiteGeom* __restrict__ out,
                                  uint32_t n) {
     pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    pack_geom_one(sites, out, i);
+}
+
+// The trainer's refresh: only the listed (active) sites; a pruned site's record is marked
+// inactive by the prune itself.
+__global__ void pack_geom_alive_kernel(const Site* __restrict__ sites, SiteGeom* __restrict__ out,
+                                       const uint32_t* __restrict__ alive, const DevState* __restrict__ state) {
+    pdl_wait();
+    const uint32_t n_alive = state->n_alive;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_alive; j += gridDim.x * blockDim.x)
+        pack_geom_one(sites, out, alive[j]);
+}
+
+__device__ __forceinline__ void pack_geom_one(const Site* __restrict__ sites, SiteGeom* __restrict__ out,
+                                              uint32_t i) {
     const float2* q = reinterpret_cast<const float2*>(sites + i);
     float2 a = q[0], b = q[1], d = q[3], e = q[4];
     uint4 v;
@@ -91,6 +109,14 @@ __global__ void pack_geom_kernel(const Site* __restrict__ sites, SiteGeom* __res
 void launch_pack_geom(const Site* sites, SiteGeom* out, uint32_t n, cudaStream_t st) {
     if (n == 0) return;
     launch_pdl(pack_geom_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st, sites, out, n);
+    note_launches(1);
+}
+
+void launch_pack_geom_alive(const Site* sites, SiteGeom* out, const uint32_t* alive, const DevState* state,
+                            uint32_t max_alive, cudaStream_t st) {
+    if (max_alive == 0) return;
+    launch_pdl(pack_geom_alive_kernel, dim3(blocks_for(max_alive, 256)), dim3(256), 0, st, sites, out, alive,
+               state);
     note_launches(1);
 }
 

@@ -53,6 +53,8 @@ struct DevState {
     uint32_t vpt_pass;  // global VPT pass index (jumpPassIndex of the reference)
     float adam_c1;      // Adam bias corrections 1 / (1 - beta^t) for t = iter + 1
     float adam_c2;
+    uint32_t n_alive;   // length of the compacted active-site list
+    uint32_t pad[3];
 };
 
 // Programmatic dependent launch: a kernel launched with the programmatic-serialization

@@ -83,6 +83,7 @@ struct sad_executor {
 namespace {
 
 sad_status_t run_fit(const Request& q, void* mem, sad_request_result_t* r) {
+    sad::NvtxRange r_nvtx("executor fit request");
     sad_trainer_t* t = nullptr;
     SAD_TRY(sad_trainer_create_in(&q.tcfg, q.w, q.h, mem, q.need, &t));
     int written = 0;
@@ -95,6 +96,7 @@ sad_status_t run_fit(const Request& q, void* mem, sad_request_result_t* r) {
 }
 
 sad_status_t run_render(const Request& q, void* mem, cudaStream_t ws) {
+    sad::NvtxRange r_nvtx("executor render request");
     char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(mem) + 255) & ~uintptr_t(255));
     float* sites = reinterpret_cast<float*>(p);
     p += a256(size_t(q.n) * 40);

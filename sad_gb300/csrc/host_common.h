@@ -12,9 +12,35 @@
 #include <cstdio>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/sad_gb300.h"
 
 namespace sad {
+
+// NVTX range in the library's own "sad_gb300" domain for the lifetime of the object: the
+// stages of a fit (init, candidate refresh, gradients, tau diffusion and Adam, prune,
+// densify, graph replays), a render from sites and executor requests, so profilers
+// (nsys, ncu --nvtx) attribute the kernels to the step that launched them.  Header-only
+// NVTX3: without an attached tool each range costs a few nanoseconds.
+inline nvtxDomainHandle_t nvtx_domain() {
+    static nvtxDomainHandle_t d = nvtxDomainCreateA("sad_gb300");
+    return d;
+}
+
+struct NvtxRange {
+    explicit NvtxRange(const char* name) {
+        nvtxEventAttributes_t a = {};
+        a.version = NVTX_VERSION;
+        a.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+        a.messageType = NVTX_MESSAGE_TYPE_ASCII;
+        a.message.ascii = name;
+        nvtxDomainRangePushEx(nvtx_domain(), &a);
+    }
+    ~NvtxRange() { nvtxDomainRangePop(nvtx_domain()); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 void set_error(const char* fmt, ...);
 void clear_error();

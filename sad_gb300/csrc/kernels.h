@@ -61,6 +61,9 @@ void launch_render_backward_raw(const uint32_t* c0, const uint32_t* c1, const fl
 // candidates.cu
 void launch_pack_sites(const Site* sites, uint16_t* packed, uint32_t n, cudaStream_t st);
 void launch_pack_geom(const Site* sites, SiteGeom* out, uint32_t n, cudaStream_t st);
+// the same for the sites of the compacted active list (state->n_alive of at most max_alive)
+void launch_pack_geom_alive(const Site* sites, SiteGeom* out, const uint32_t* alive,
+                            const DevState* state, uint32_t max_alive, cudaStream_t st);
 void launch_vpt_packed(const VptParams& prm, const uint16_t* packed, cudaStream_t st);
 void launch_vpt_geom(const VptParams& prm, const SiteGeom* geom, cudaStream_t st);
 void launch_jfa_seed(uint32_t* cand0, const Site* sites, uint32_t n, int w, int h, int ds,
@@ -117,15 +120,16 @@ void launch_gradients_prepared(const GradParams& p, const SiteGeom* geom, const 
 void launch_tau_diffuse_raw(const uint32_t* c0, const uint32_t* c1, const Site* sites,
                             const float* raw, const float* gin, float* gout, uint32_t n,
                             float lambda, int w, int h, int ds, cudaStream_t st);
-// trainer form, first Jacobi pass: raw log-tau gradient from slot 2 of the fixed-point
-// records; records each active site's neighbour list nbr[n][8], raw[n] and active[n]
+// trainer form, first Jacobi pass over the compacted active list (alive, state->n_alive
+// entries, at most max_alive): raw log-tau gradient from slot 2 of the fixed-point
+// records; records each listed site's neighbour list nbr[n][8] and raw[n]
 void launch_tau_first_pass(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
-                           const long long* fix12, uint32_t* nbr, float* raw, uint8_t* active,
-                           float* gout, uint32_t n, const DevState* state, int iterations, int w,
-                           int h, int ds, cudaStream_t st);
+                           const long long* fix12, uint32_t* nbr, float* raw, const uint32_t* alive,
+                           float* gout, uint32_t n, uint32_t max_alive, const DevState* state,
+                           int iterations, int w, int h, int ds, cudaStream_t st);
 // trainer form, middle passes from the recorded lists
-void launch_tau_list_pass(const uint32_t* nbr, const float* raw, const uint8_t* active,
-                          const float* gin, float* gout, uint32_t n, const DevState* state,
+void launch_tau_list_pass(const uint32_t* nbr, const float* raw, const uint32_t* alive,
+                          const float* gin, float* gout, uint32_t max_alive, const DevState* state,
                           int iterations, cudaStream_t st);
 struct AdamHyper {
     float lr_pos, lr_tau, lr_radius, lr_color, lr_dir, lr_aniso;
@@ -133,13 +137,13 @@ struct AdamHyper {
 };
 void launch_adam_soa(Site* sites, float* adam, const float* const g[10], const AdamHyper& hp,
                      uint32_t t, uint32_t n, int w, int h, cudaStream_t st);
-// trainer form: last tau pass (from tau_gin and the lists) fused with Adam on the
-// fixed-point records (slots 0-9 consumed and zeroed), refreshing SiteGeom/SiteColor;
-// t = state->iter + 1; inactive sites untouched
+// trainer form over the compacted active list: last tau pass (from tau_gin and the lists)
+// fused with Adam on the fixed-point records (slots 0-9 consumed and zeroed), refreshing
+// SiteGeom/SiteColor; t = state->iter + 1
 void launch_adam_train(Site* sites, float* adam, long long* fix12, const uint32_t* nbr,
-                       const float* raw, const uint8_t* active, const float* tau_gin,
+                       const float* raw, const uint32_t* alive, const float* tau_gin,
                        SiteGeom* geom, SiteColor* color, const AdamHyper& hp,
-                       const DevState* state, int iterations, uint32_t n, int w, int h,
+                       const DevState* state, int iterations, uint32_t max_alive, int w, int h,
                        cudaStream_t st);
 void launch_clear_f32(float* buf, size_t count, cudaStream_t st);
 // iteration counter, VPT pass counter and the next iteration's Adam bias corrections
@@ -151,6 +155,10 @@ void launch_advance_state(DevState* state, uint32_t vpt_passes, float beta1, flo
 size_t radix_sort_temp_bytes(uint32_t count);
 void launch_radix_sort(uint32_t* pairs, uint32_t count, uint32_t max_key_exclusive, void* temp,
                        cudaStream_t st);
+// The same sort of *dev_count pairs (at most max_count; temp sized for max_count), the
+// count read on the device so a captured graph serves any count.
+void launch_radix_sort_dev(uint32_t* pairs, uint32_t max_count, const uint32_t* dev_count,
+                           uint32_t max_key_exclusive, void* temp, cudaStream_t st);
 // exclusive scan of `count` words in place by one CTA; *total (nullable) = sum
 void launch_scan_single(uint32_t* data, uint32_t count, uint32_t* total, cudaStream_t st);
 
@@ -167,10 +175,19 @@ void launch_prune_pairs_fixed(const Site* sites, long long* fix12, float fix_mul
                               uint32_t n, float delta_norm, uint32_t pair_count, cudaStream_t st);
 void launch_write_indices(const uint32_t* pairs, uint32_t* idx, uint32_t k, cudaStream_t st);
 void launch_prune_by_index(Site* sites, const uint32_t* idx, uint32_t k, cudaStream_t st);
-// trainer form: prune the first prune_k[state->iter] entries of sorted pairs, also in geom
-void launch_prune_sorted_train(Site* sites, SiteGeom* geom, const uint32_t* pairs,
+// trainer form over the compacted active list (state->n_alive pairs, at most max_alive)
+void launch_prune_pairs_alive(long long* fix12, float fix_mul, uint32_t* pairs, const uint32_t* alive,
+                              const DevState* state, uint32_t max_alive, float delta_norm, cudaStream_t st);
+// trainer form: prune the first prune_k[state->iter] entries of sorted pairs, also in the
+// prepared and the VPT geometry
+void launch_prune_sorted_train(Site* sites, SiteGeom* geom, SiteGeom* vgeom, const uint32_t* pairs,
                                const uint32_t* prune_k, const DevState* state, uint32_t max_k,
                                cudaStream_t st);
+// stream compaction of the active set: alive = ascending active slots of [0, n) (prepared
+// geometry px >= 0), *n_alive = their number; block_counts holds compact_blocks(n) words
+uint32_t compact_blocks(uint32_t n);
+void launch_compact_active(const SiteGeom* geom, uint32_t n, uint32_t* block_counts, uint32_t* alive,
+                           uint32_t* n_alive, cudaStream_t st);
 void launch_split(Site* sites, float* adam, const uint32_t* split_idx, uint32_t num,
                   const float* const stats[7], uint32_t cur, const float* target, int w, int h,
                   cudaStream_t st);

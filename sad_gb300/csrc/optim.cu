@@ -80,13 +80,20 @@ __device__ __forceinline__ float tau_lambda(uint32_t iter, int iterations) {
 // set of positions, so the first pass records each active site's neighbour list (the
 // distinct active candidates at its texel, in candidate order) and the raw gradient as a
 // float; the middle passes read the list; the last pass runs inside the Adam kernel.
-// Inactive sites are skipped: their diffused value is never read (a neighbour must be
-// active, and Adam skips inactive sites).
+// Every pass walks the compacted list of active sites (state->n_alive entries): an
+// inactive site's diffused value is never read (a neighbour must be active, and Adam
+// skips inactive sites).
 struct TauLists {
-    uint4* nbr;        // [n][2] neighbour ids, kEmpty-padded
-    float* raw;        // [n] raw log-tau gradient (float)
-    uint8_t* active;   // [n] 1 = active site
+    uint4* nbr;            // [n][2] neighbour ids, kEmpty-padded
+    float* raw;            // [n] raw log-tau gradient (float)
+    const uint32_t* alive; // the compacted active list
 };
+
+__device__ __forceinline__ void tau_first_one(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
+                                              const SiteGeom* __restrict__ geom,
+                                              const long long* __restrict__ fix12, const TauLists& tl,
+                                              float* __restrict__ gout, uint32_t n, uint32_t i,
+                                              float lambda, int w, int h, int ds);
 
 __global__ void tau_first_pass_kernel(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
                                       const SiteGeom* __restrict__ geom,
@@ -95,13 +102,20 @@ __global__ void tau_first_pass_kernel(const uint4* __restrict__ c0, const uint4*
                                       const DevState* __restrict__ state, int iterations, int w,
                                       int h, int ds) {
     pdl_wait();
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float2 sp = __ldg(reinterpret_cast<const float2*>(geom + i));
-    bool act = sp.x >= 0.0f;
-    tl.active[i] = act ? 1 : 0;
-    if (!act) return;
+    const uint32_t n_alive = state->n_alive;
     const float lambda = tau_lambda(state->iter, iterations);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_alive; j += gridDim.x * blockDim.x) {
+        const uint32_t i = tl.alive[j];
+        tau_first_one(c0, c1, geom, fix12, tl, gout, n, i, lambda, w, h, ds);
+    }
+}
+
+__device__ __forceinline__ void tau_first_one(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
+                                              const SiteGeom* __restrict__ geom,
+                                              const long long* __restrict__ fix12, const TauLists& tl,
+                                              float* __restrict__ gout, uint32_t n, uint32_t i,
+                                              float lambda, int w, int h, int ds) {
+    float2 sp = __ldg(reinterpret_cast<const float2*>(geom + i));
     const float r = from_fix(fix12[static_cast<size_t>(i) * 12 + 2]);
     tl.raw[i] = r;
     float inv = 1.0f / fmaxf(static_cast<float>(ds), 1.0f);
@@ -156,33 +170,36 @@ __device__ __forceinline__ float tau_list_pass(const TauLists& tl, const float* 
 }
 
 __global__ void tau_list_pass_kernel(TauLists tl, const float* __restrict__ gin,
-                                     float* __restrict__ gout, uint32_t n,
-                                     const DevState* __restrict__ state, int iterations) {
+                                     float* __restrict__ gout, const DevState* __restrict__ state,
+                                     int iterations) {
     pdl_wait();
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !tl.active[i]) return;
-    gout[i] = tau_list_pass(tl, gin, i, tau_lambda(state->iter, iterations));
+    const uint32_t n_alive = state->n_alive;
+    const float lambda = tau_lambda(state->iter, iterations);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_alive; j += gridDim.x * blockDim.x) {
+        const uint32_t i = tl.alive[j];
+        gout[i] = tau_list_pass(tl, gin, i, lambda);
+    }
 }
 
 void launch_tau_first_pass(const uint32_t* c0, const uint32_t* c1, const SiteGeom* geom,
-                           const long long* fix12, uint32_t* nbr, float* raw, uint8_t* active,
-                           float* gout, uint32_t n, const DevState* state, int iterations, int w,
-                           int h, int ds, cudaStream_t st) {
-    if (n == 0) return;
-    TauLists tl{reinterpret_cast<uint4*>(nbr), raw, active};
-    launch_pdl(tau_first_pass_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st,
+                           const long long* fix12, uint32_t* nbr, float* raw, const uint32_t* alive,
+                           float* gout, uint32_t n, uint32_t max_alive, const DevState* state,
+                           int iterations, int w, int h, int ds, cudaStream_t st) {
+    if (max_alive == 0) return;
+    TauLists tl{reinterpret_cast<uint4*>(nbr), raw, alive};
+    launch_pdl(tau_first_pass_kernel, dim3(blocks_for(max_alive, 256)), dim3(256), 0, st,
                reinterpret_cast<const uint4*>(c0), reinterpret_cast<const uint4*>(c1), geom, fix12, tl, gout, n,
                state, iterations, w, h, ds);
     note_launches(1);
 }
 
-void launch_tau_list_pass(const uint32_t* nbr, const float* raw, const uint8_t* active,
-                          const float* gin, float* gout, uint32_t n, const DevState* state,
+void launch_tau_list_pass(const uint32_t* nbr, const float* raw, const uint32_t* alive,
+                          const float* gin, float* gout, uint32_t max_alive, const DevState* state,
                           int iterations, cudaStream_t st) {
-    if (n == 0) return;
-    TauLists tl{reinterpret_cast<uint4*>(const_cast<uint32_t*>(nbr)), const_cast<float*>(raw),
-                const_cast<uint8_t*>(active)};
-    launch_pdl(tau_list_pass_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st, tl, gin, gout, n, state, iterations);
+    if (max_alive == 0) return;
+    TauLists tl{reinterpret_cast<uint4*>(const_cast<uint32_t*>(nbr)), const_cast<float*>(raw), alive};
+    launch_pdl(tau_list_pass_kernel, dim3(blocks_for(max_alive, 256)), dim3(256), 0, st, tl, gin, gout, state,
+               iterations);
     note_launches(1);
 }
 
@@ -336,15 +353,30 @@ void launch_adam_soa(Site* sites, float* adam, const float* const g[10], const A
 // which are consumed and cleared (slots 0-9; slots 10-11, the removal delta, belong to the
 // prune step), then the refreshed SiteGeom / SiteColor records.  Inactive sites carry no
 // gradient and are left untouched.
+__device__ __forceinline__ void adam_train_one(Site* __restrict__ sites, float* __restrict__ adam,
+                                               long long* __restrict__ fix12, const TauLists& tl,
+                                               const float* __restrict__ tau_gin, SiteGeom* __restrict__ geom,
+                                               SiteColor* __restrict__ color, const AdamHyper& hp,
+                                               const DevState* __restrict__ state, int iterations, int w, int h,
+                                               uint32_t i);
+
 __global__ void adam_train_kernel(Site* __restrict__ sites, float* __restrict__ adam,
                                   long long* __restrict__ fix12, TauLists tl,
                                   const float* __restrict__ tau_gin, SiteGeom* __restrict__ geom,
                                   SiteColor* __restrict__ color, AdamHyper hp,
-                                  const DevState* __restrict__ state, int iterations, uint32_t n,
-                                  int w, int h) {
+                                  const DevState* __restrict__ state, int iterations, int w, int h) {
     pdl_wait();
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !tl.active[i]) return;
+    const uint32_t n_alive = state->n_alive;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_alive; j += gridDim.x * blockDim.x)
+        adam_train_one(sites, adam, fix12, tl, tau_gin, geom, color, hp, state, iterations, w, h, tl.alive[j]);
+}
+
+__device__ __forceinline__ void adam_train_one(Site* __restrict__ sites, float* __restrict__ adam,
+                                               long long* __restrict__ fix12, const TauLists& tl,
+                                               const float* __restrict__ tau_gin, SiteGeom* __restrict__ geom,
+                                               SiteColor* __restrict__ color, const AdamHyper& hp,
+                                               const DevState* __restrict__ state, int iterations, int w, int h,
+                                               uint32_t i) {
     const float tau_g = tau_list_pass(tl, tau_gin, i, tau_lambda(state->iter, iterations));
     float norm = 1.0f / static_cast<float>(w * h);
     longlong2* gq = reinterpret_cast<longlong2*>(fix12 + static_cast<size_t>(i) * 12);
@@ -369,15 +401,14 @@ __global__ void adam_train_kernel(Site* __restrict__ sites, float* __restrict__ 
 }
 
 void launch_adam_train(Site* sites, float* adam, long long* fix12, const uint32_t* nbr,
-                       const float* raw, const uint8_t* active, const float* tau_gin,
+                       const float* raw, const uint32_t* alive, const float* tau_gin,
                        SiteGeom* geom, SiteColor* color, const AdamHyper& hp,
-                       const DevState* state, int iterations, uint32_t n, int w, int h,
+                       const DevState* state, int iterations, uint32_t max_alive, int w, int h,
                        cudaStream_t st) {
-    if (n == 0) return;
-    TauLists tl{reinterpret_cast<uint4*>(const_cast<uint32_t*>(nbr)), const_cast<float*>(raw),
-                const_cast<uint8_t*>(active)};
-    launch_pdl(adam_train_kernel, dim3(blocks_for(n, 256)), dim3(256), 0, st, sites, adam, fix12, tl, tau_gin,
-               geom, color, hp, state, iterations, n, w, h);
+    if (max_alive == 0) return;
+    TauLists tl{reinterpret_cast<uint4*>(const_cast<uint32_t*>(nbr)), const_cast<float*>(raw), alive};
+    launch_pdl(adam_train_kernel, dim3(blocks_for(max_alive, 256)), dim3(256), 0, st, sites, adam, fix12, tl,
+               tau_gin, geom, color, hp, state, iterations, w, h);
     note_launches(1);
 }
 

@@ -168,6 +168,7 @@ extern "C" sad_status_t sad_render_from_sites(const sad_render_config_t* cfg, co
                                               uint32_t n, int width, int height, float* out_rgb,
                                               void* scratch, size_t scratch_bytes,
                                               sad_stream_t stream) {
+    NvtxRange r_nvtx("render from sites");
     clear_error();
     return render_from_sites_impl(cfg, sites_f, n, width, height, out_rgb, scratch, scratch_bytes, stream,
                                   nullptr);

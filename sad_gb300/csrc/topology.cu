@@ -90,6 +90,34 @@ __global__ void prune_pairs_fixed_kernel(const Site* __restrict__ sites, long lo
     pairs[i] = o;
 }
 
+// Trainer form over the compacted active list (grid-stride; any grid size is correct):
+// pair j is (key, alive[j]) for the n_alive listed sites (the same sorted prefix as pairs over every slot, where inactive
+// slots key 0xFFFFFFFF), and their removal records are consumed.
+__global__ void prune_pairs_alive_kernel(long long* __restrict__ fix12, float inv_mul,
+                                         uint2* __restrict__ pairs, const uint32_t* __restrict__ alive,
+                                         const DevState* __restrict__ state, float delta_norm) {
+    pdl_wait();
+    const uint32_t n_alive = state->n_alive;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_alive; j += gridDim.x * blockDim.x) {
+        const uint32_t i = alive[j];
+        longlong2* r = reinterpret_cast<longlong2*>(fix12 + static_cast<size_t>(i) * 12 + 10);
+        longlong2 v = *r;
+        *r = make_longlong2(0, 0);
+        float removal = static_cast<float>(v.y) * 1.0e6f + from_fix(v.x) * inv_mul;
+        float delta = removal * delta_norm;
+        pairs[j] = isfinite(delta) ? make_uint2(__float_as_uint(fmaxf(delta, 0.0f)), i)
+                                   : make_uint2(kEmpty, kEmpty);
+    }
+}
+
+void launch_prune_pairs_alive(long long* fix12, float fix_mul, uint32_t* pairs, const uint32_t* alive,
+                              const DevState* state, uint32_t max_alive, float delta_norm, cudaStream_t st) {
+    if (max_alive == 0) return;
+    launch_pdl(prune_pairs_alive_kernel, dim3(blocks_for(max_alive, 256)), dim3(256), 0, st, fix12,
+               1.0f / fix_mul, reinterpret_cast<uint2*>(pairs), alive, state, delta_norm);
+    note_launches(1);
+}
+
 void launch_prune_pairs_fixed(const Site* sites, long long* fix12, float fix_mul, uint32_t* pairs,
                               uint32_t n, float delta_norm, uint32_t pair_count, cudaStream_t st) {
     if (pair_count == 0) return;
@@ -129,10 +157,13 @@ void launch_prune_by_index(Site* sites, const uint32_t* idx, uint32_t k, cudaStr
 
 // Trainer form: write-indices + prune fused; the count comes from the host-planned
 // per-iteration table (the schedule is fixed before the fit starts).
+// The pruned sites are marked inactive in the site records, the prepared geometry and
+// the VPT geometry (the refresh repacks only listed sites).
 __global__ void prune_sorted_kernel(Site* __restrict__ sites, SiteGeom* __restrict__ geom,
-                                    const uint2* __restrict__ pairs,
+                                    SiteGeom* __restrict__ vgeom, const uint2* __restrict__ pairs,
                                     const uint32_t* __restrict__ prune_k,
                                     const DevState* __restrict__ state) {
+    pdl_wait();
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t k = prune_k[state->iter];
     if (i >= k) return;
@@ -142,14 +173,16 @@ __global__ void prune_sorted_kernel(Site* __restrict__ sites, SiteGeom* __restri
     sites[s].py = -1.0f;
     geom[s].px = -1.0f;
     geom[s].py = -1.0f;
+    vgeom[s].px = -1.0f;
+    vgeom[s].py = -1.0f;
 }
 
-void launch_prune_sorted_train(Site* sites, SiteGeom* geom, const uint32_t* pairs,
+void launch_prune_sorted_train(Site* sites, SiteGeom* geom, SiteGeom* vgeom, const uint32_t* pairs,
                                const uint32_t* prune_k, const DevState* state, uint32_t max_k,
                                cudaStream_t st) {
     if (max_k == 0) return;
-    prune_sorted_kernel<<<blocks_for(max_k, 256), 256, 0, st>>>(
-        sites, geom, reinterpret_cast<const uint2*>(pairs), prune_k, state);
+    launch_pdl(prune_sorted_kernel, dim3(blocks_for(max_k, 256)), dim3(256), 0, st, sites, geom, vgeom,
+               reinterpret_cast<const uint2*>(pairs), prune_k, state);
     note_launches(1);
 }
 
@@ -646,6 +679,118 @@ void launch_ssim(const float* ren, const float* tgt, const float* mask, float* a
     note_launches(1);
 }
 
+// ---------------------------------------------------------------------------
+// stream compaction of the active set: the ascending list of the active sites of [0, n)
+// and its length (in DevState), rebuilt after init, densify and every prune.  The site
+// records themselves stay in place: candidate fields, tile maps and the Hilbert order
+// keep naming sites by their slot, and the per-site kernels walk the list.
+// ---------------------------------------------------------------------------
+constexpr int kCompactThreads = 256;
+constexpr int kCompactPer = 4;  // sites per thread
+constexpr int kCompactBlock = kCompactThreads * kCompactPer;
+
+uint32_t compact_blocks(uint32_t n) { return (n + kCompactBlock - 1) / kCompactBlock; }
+
+// Active flags of sites base .. base+3: px[i * stride] >= 0 (stride in floats: 8 for the
+// prepared geometry, 10 for site records).
+__device__ __forceinline__ uint32_t compact_flags(const float* __restrict__ px, uint32_t stride, uint32_t n,
+                                                  uint32_t base) {
+    uint32_t f = 0;
+#pragma unroll
+    for (int k = 0; k < kCompactPer; ++k) {
+        const uint32_t i = base + k;
+        if (i < n && __ldg(px + static_cast<size_t>(i) * stride) >= 0.0f) f |= 1u << k;
+    }
+    return f;
+}
+
+__global__ void __launch_bounds__(kCompactThreads) compact_count_kernel(const float* __restrict__ px,
+                                                                        uint32_t stride, uint32_t n,
+                                                                        uint32_t* __restrict__ counts) {
+    pdl_wait();
+    __shared__ uint32_t warp_sums[kCompactThreads / 32];
+    const uint32_t base = blockIdx.x * kCompactBlock + threadIdx.x * kCompactPer;
+    uint32_t c = __popc(compact_flags(px, stride, n, base));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+#pragma unroll
+        for (int w = 0; w < kCompactThreads / 32; ++w) t += warp_sums[w];
+        counts[blockIdx.x] = t;
+    }
+}
+
+// Each block sums the counts of the blocks before it (a few hundred words even at a
+// million sites), scans its own flags and writes its slots in order; the last block also
+// writes the total.
+__global__ void __launch_bounds__(kCompactThreads) compact_write_kernel(const float* __restrict__ px,
+                                                                        uint32_t stride, uint32_t n,
+                                                                        const uint32_t* __restrict__ counts,
+                                                                        uint32_t* __restrict__ alive,
+                                                                        uint32_t* __restrict__ n_alive) {
+    pdl_wait();
+    __shared__ uint32_t warp_sums[kCompactThreads / 32];
+    __shared__ uint32_t s_before;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    {
+        uint32_t b = 0;
+        for (uint32_t k = tid; k < blockIdx.x; k += kCompactThreads) b += counts[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) b += __shfl_down_sync(0xffffffffu, b, o);
+        if (lane == 0) warp_sums[warp] = b;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t t = 0;
+#pragma unroll
+            for (int w = 0; w < kCompactThreads / 32; ++w) t += warp_sums[w];
+            s_before = t;
+            if (blockIdx.x == gridDim.x - 1) *n_alive = t + counts[blockIdx.x];
+        }
+        __syncthreads();
+    }
+    const uint32_t base = blockIdx.x * kCompactBlock + tid * kCompactPer;
+    const uint32_t f = compact_flags(px, stride, n, base);
+    const uint32_t c = __popc(f);
+    uint32_t x = c;  // inclusive scan over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += t;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    uint32_t before = s_before;
+#pragma unroll
+    for (int w = 0; w < kCompactThreads / 32; ++w)
+        if (w < warp) before += warp_sums[w];
+    uint32_t out = before + x - c;
+#pragma unroll
+    for (int k = 0; k < kCompactPer; ++k)
+        if (f >> k & 1u) alive[out++] = base + k;
+}
+
+static void launch_compact(const float* px, uint32_t stride, uint32_t n, uint32_t* block_counts,
+                           uint32_t* alive, uint32_t* n_alive, cudaStream_t st) {
+    const uint32_t blocks = std::max(1u, compact_blocks(n));
+    launch_pdl(compact_count_kernel, dim3(blocks), dim3(kCompactThreads), 0, st, px, stride, n, block_counts);
+    launch_pdl(compact_write_kernel, dim3(blocks), dim3(kCompactThreads), 0, st, px, stride, n,
+               static_cast<const uint32_t*>(block_counts), alive, n_alive);
+    note_launches(2);
+}
+
+void launch_compact_active(const SiteGeom* geom, uint32_t n, uint32_t* block_counts, uint32_t* alive,
+                           uint32_t* n_alive, cudaStream_t st) {
+    launch_compact(reinterpret_cast<const float*>(geom), 8u, n, block_counts, alive, n_alive, st);
+}
+
+void launch_compact_sites(const Site* sites, uint32_t n, uint32_t* block_counts, uint32_t* alive,
+                          uint32_t* n_alive, cudaStream_t st) {
+    launch_compact(reinterpret_cast<const float*>(sites), 10u, n, block_counts, alive, n_alive, st);
+}
+
 __global__ void count_active_kernel(const Site* __restrict__ sites, uint32_t* __restrict__ count,
                                     uint32_t n) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1087,4 +1232,21 @@ extern "C" sad_status_t sad_count_active_sites(const float* sites, uint32_t* cou
     SAD_REQUIRE(count && (sites || site_count == 0), "sad_count_active_sites: null buffer");
     launch_count_active(reinterpret_cast<const Site*>(sites), count, site_count, as_stream(stream));
     return check_launch("sad_count_active_sites");
+}
+
+extern "C" size_t sad_compact_active_scratch_bytes(uint32_t site_count) {
+    return (static_cast<size_t>(std::max(1u, compact_blocks(site_count))) * 4 + 255) & ~size_t(255);
+}
+
+extern "C" sad_status_t sad_compact_active(const float* sites, uint32_t site_count, uint32_t* alive_out,
+                                           uint32_t* count_dev, void* scratch, size_t scratch_bytes,
+                                           sad_stream_t stream) {
+    clear_error();
+    SAD_REQUIRE(count_dev, "sad_compact_active: null count");
+    SAD_REQUIRE(site_count == 0 || (sites && alive_out), "sad_compact_active: null buffer");
+    SAD_REQUIRE(scratch && scratch_bytes >= sad_compact_active_scratch_bytes(site_count),
+                "sad_compact_active: scratch smaller than sad_compact_active_scratch_bytes(site_count)");
+    launch_compact_sites(reinterpret_cast<const Site*>(sites), site_count, static_cast<uint32_t*>(scratch),
+                         alive_out, count_dev, as_stream(stream));
+    return check_launch("sad_compact_active");
 }

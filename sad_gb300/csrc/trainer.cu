@@ -72,7 +72,11 @@ struct sad_trainer {
     float* tau_b = nullptr;
     uint32_t* tau_nbr = nullptr;  // [cap][8] neighbour lists of the tau passes
     float* tau_raw = nullptr;
-    uint8_t* tau_active = nullptr;
+    // stream compaction of the active set: ascending active slots (state->n_alive of them),
+    // walked by the per-site kernels; rebuilt after init, densify and every prune
+    uint32_t* alive = nullptr;
+    uint32_t* alive_blocks = nullptr;
+    uint32_t alive_hint = 0;  // thread count of the per-site kernels' grids
     uint32_t* pairs = nullptr;
     void* sort_temp = nullptr;
     uint32_t* idx = nullptr;
@@ -209,9 +213,21 @@ static VptParams vpt_params(sad_trainer* t) {
     return p;
 }
 
+// Thread count of the per-site kernels' grids: the buffer's site count (the kernels loop
+// over the compacted list, so the grid only has to be large enough for the first
+// iterations; later blocks beyond the list return at once), so the captured graphs serve
+// the whole fit.
+static uint32_t alive_grid_hint(const sad_trainer* t) { return std::max<uint32_t>(1u, t->n); }
+
+static uint32_t* n_alive_ptr(sad_trainer* t) { return &t->state->n_alive; }
+
+static void launch_compact(sad_trainer* t, cudaStream_t s) {
+    launch_compact_active(t->geom, t->n, t->alive_blocks, t->alive, n_alive_ptr(t), s);
+}
+
 // VPT passes from field `src` into the spare fields; returns the final field index.
 static int launch_refresh(sad_trainer* t, int src, cudaStream_t s) {
-    launch_pack_geom(t->sites, t->vgeom, t->n, s);
+    launch_pack_geom_alive(t->sites, t->vgeom, t->alive, t->state, t->alive_hint, s);
     int o[2], k = 0;
     for (int b = 0; b < 3; ++b)
         if (b != src) o[k++] = b;
@@ -270,6 +286,7 @@ static int iteration_body(sad_trainer* t, bool upd, bool prune, int field, int a
                           cudaStream_t s) {
     int next = field;
     if (upd) {
+        NvtxRange r("candidate refresh (VPT, tile registration)");
         cudaEventRecord(t->ev_fork, s);
         cudaStreamWaitEvent(t->side, t->ev_fork, 0);
         next = launch_refresh(t, field, t->side);
@@ -280,39 +297,50 @@ static int iteration_body(sad_trainer* t, bool upd, bool prune, int field, int a
                                t->inv_s2, t->n, t->w, t->h, t->cw, t->ch, s);
     bool timed = t->timing && t->tev_used + 2 <= t->tev.size();
     if (timed) cudaEventRecord(t->tev[t->tev_used], s);
-    launch_gradients_step(t, field, prune, s);
+    {
+        NvtxRange r_grad("gradients");
+        launch_gradients_step(t, field, prune, s);
+    }
     if (timed) {
         cudaEventRecord(t->tev[t->tev_used + 1], s);
         t->tev_used += 2;
     }
     if (upd) cudaStreamWaitEvent(s, t->ev_join, 0);
-    // 4 Jacobi passes: grads slot 2 -> A -> B -> A -> (inside Adam)
-    launch_tau_first_pass(t->cand0[next], t->cand1[next], t->geom, t->grads, t->tau_nbr, t->tau_raw,
-                          t->tau_active, t->tau_a, t->n, t->state, t->cfg.iterations, t->cw, t->ch,
-                          t->ds, s);
-    launch_tau_list_pass(t->tau_nbr, t->tau_raw, t->tau_active, t->tau_a, t->tau_b, t->n, t->state,
-                         t->cfg.iterations, s);
-    launch_tau_list_pass(t->tau_nbr, t->tau_raw, t->tau_active, t->tau_b, t->tau_a, t->n, t->state,
-                         t->cfg.iterations, s);
-    AdamHyper hp{t->cfg.lr_pos * t->cfg.lr_scale, t->cfg.lr_tau * t->cfg.lr_scale,
-                 t->cfg.lr_radius * t->cfg.lr_scale, t->cfg.lr_color * t->cfg.lr_scale,
-                 t->cfg.lr_dir * t->cfg.lr_scale, t->cfg.lr_aniso * t->cfg.lr_scale,
-                 t->cfg.beta1, t->cfg.beta2, t->cfg.eps};
-    launch_adam_train(t->sites, t->adam, t->grads, t->tau_nbr, t->tau_raw, t->tau_active, t->tau_a,
-                      t->geom, t->color, hp, t->state, t->cfg.iterations, t->n, t->w, t->h, s);
+    // 4 Jacobi passes: grads slot 2 -> A -> B -> A -> (inside Adam), over the active list
+    const uint32_t hint = t->alive_hint;
+    {
+        NvtxRange r_site("tau diffusion and Adam");
+        launch_tau_first_pass(t->cand0[next], t->cand1[next], t->geom, t->grads, t->tau_nbr, t->tau_raw,
+                              t->alive, t->tau_a, t->n, hint, t->state, t->cfg.iterations, t->cw, t->ch,
+                              t->ds, s);
+        launch_tau_list_pass(t->tau_nbr, t->tau_raw, t->alive, t->tau_a, t->tau_b, hint, t->state,
+                             t->cfg.iterations, s);
+        launch_tau_list_pass(t->tau_nbr, t->tau_raw, t->alive, t->tau_b, t->tau_a, hint, t->state,
+                             t->cfg.iterations, s);
+        AdamHyper hp{t->cfg.lr_pos * t->cfg.lr_scale, t->cfg.lr_tau * t->cfg.lr_scale,
+                     t->cfg.lr_radius * t->cfg.lr_scale, t->cfg.lr_color * t->cfg.lr_scale,
+                     t->cfg.lr_dir * t->cfg.lr_scale, t->cfg.lr_aniso * t->cfg.lr_scale,
+                     t->cfg.beta1, t->cfg.beta2, t->cfg.eps};
+        launch_adam_train(t->sites, t->adam, t->grads, t->tau_nbr, t->tau_raw, t->alive, t->tau_a,
+                          t->geom, t->color, hp, t->state, t->cfg.iterations, hint, t->w, t->h, s);
+    }
     if (prune) {
+        // score, sort and prune the active list (the same sorted prefix as over every slot:
+        // inactive slots key last), then compact the list again
+        NvtxRange r("prune (score, sort, mark, compact)");
         float delta_norm = 1.0f / std::max(1.0f, t->mask_sum);
-        launch_prune_pairs_fixed(t->sites, t->grads, t->removal_mul, t->pairs, t->n, delta_norm,
-                                 t->cap, s);
-        launch_radix_sort(t->pairs, t->cap, 0xFFFFFFFFu, t->sort_temp, s);
-        launch_prune_sorted_train(t->sites, t->geom, t->pairs, t->prune_k, t->state,
+        launch_prune_pairs_alive(t->grads, t->removal_mul, t->pairs, t->alive, t->state, hint, delta_norm, s);
+        launch_radix_sort_dev(t->pairs, t->n, n_alive_ptr(t), 0xFFFFFFFFu, t->sort_temp, s);
+        launch_prune_sorted_train(t->sites, t->geom, t->vgeom, t->pairs, t->prune_k, t->state,
                                   SAD_MAX_SPLIT_INDICES, s);
+        launch_compact(t, s);
     }
     launch_advance_state(t->state, static_cast<uint32_t>(adv_passes), t->cfg.beta1, t->cfg.beta2, s);
     return next;
 }
 
 static sad_status_t run_densify(sad_trainer* t, const IterPlan& p, cudaStream_t s) {
+    NvtxRange r("densify (statistics, score, sort, split, compact)");
     // site statistics on the current field, score, sort, split (sad_cuda.cu:2232-2292)
     float* st[8];
     for (int k = 0; k < 8; ++k) st[k] = t->stats + static_cast<size_t>(k) * t->cap;
@@ -328,6 +356,8 @@ static sad_status_t run_densify(sad_trainer* t, const IterPlan& p, cudaStream_t 
     t->n += p.split_k;
     t->active += static_cast<int>(p.split_k);
     launch_prepare_sites(t->sites, t->geom, t->color, t->n, s);
+    launch_compact(t, s);
+    t->alive_hint = alive_grid_hint(t);
     drop_graphs(t);  // site count changed
     return check_launch("trainer densify");
 }
@@ -431,7 +461,8 @@ static size_t carve_trainer(sad_trainer* t, void* base) {
     c.take(t->tau_b, cap);
     c.take(t->tau_nbr, cap * 8);
     c.take(t->tau_raw, cap);
-    c.take(t->tau_active, cap);
+    c.take(t->alive, cap);
+    c.take(t->alive_blocks, std::max<uint32_t>(1u, compact_blocks(t->cap)));
     c.take(t->pairs, cap * 2);
     c.take(t->idx, SAD_MAX_SPLIT_INDICES);
     for (int b = 0; b < 3; ++b) {
@@ -609,6 +640,7 @@ __global__ void fill_inactive_kernel(sad::Site* sites, uint32_t from, uint32_t t
 extern "C" sad_status_t sad_trainer_init(sad_trainer_t* t, const float* sites_host, int n) {
     clear_error();
     SAD_REQUIRE(t, "sad_trainer_init: null trainer");
+    NvtxRange r_init("fit init (sites, candidates, plan)");
     cudaStream_t s = t->st;
     uint32_t n0;
     int active;
@@ -647,6 +679,11 @@ extern "C" sad_status_t sad_trainer_init(sad_trainer_t* t, const float* sites_ho
     t->iter = 0;
     t->cur = 0;
     t->hilbert_ready = false;
+    // the VPT geometry of every slot once (inactive slots stay marked; refreshes repack the
+    // active list) and the first active list
+    launch_pack_geom(t->sites, t->vgeom, n0, s);
+    launch_compact(t, s);
+    t->alive_hint = alive_grid_hint(t);
     launch_init_candidates(t->cand0[0], t->cand1[0], n0, 0u, t->cfg.init_per_pixel ? 1 : 0, t->cw, t->ch, s);
     launch_jfa_seed(t->cand0[0], t->sites, n0, t->cw, t->ch, t->ds, s);
     launch_register_tiles(t->cand0[0], t->cand1[0], n0, t->w, t->h, t->cw, t->ch, t->tmap[0], s);
@@ -682,6 +719,7 @@ extern "C" sad_status_t sad_trainer_run(sad_trainer_t* t, int end) {
     bool use_h = c.cand_hilbert_probes > 0 && c.cand_hilbert_window > 0;
     bool eager = !c.use_graphs || t->timing;
     t->tev_used = 0;
+    NvtxRange r_run(eager ? "fit iterations (eager)" : "fit iterations (graph replays)");
     for (int it = t->iter; it < end; ++it) {
         const IterPlan& p = t->plan[it];
         if (p.upd && use_h && (!t->hilbert_ready || t->hilbert_count != t->n))

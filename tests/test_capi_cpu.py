@@ -102,13 +102,15 @@ def test_default_config_is_the_reference_training_config(sadlib):
 
 
 def test_torch_op_schemas_registered():
+    """Every operator of the reference extension is registered with its exact schema."""
     import torch
     from sad_gb300 import torch_ops
+    from torch_schemas import SCHEMAS
     assert torch_ops.register()
-    assert len(torch_ops.SCHEMAS) == 24
-    for name in torch_ops.SCHEMAS:
+    assert len(SCHEMAS) == 24
+    for name, schema in SCHEMAS.items():
         op = getattr(torch.ops.sad, name)
-        assert str(op.default._schema).startswith("sad::" + name)
+        assert str(op.default._schema) == "sad::" + schema, name
 
 
 def test_sad_ops_package_mirrors_the_reference_extension():

@@ -268,13 +268,16 @@ def _fixed_gradients(w, h, n, c0, c1, img, rendered, mask, sites, removal, ssim)
 @pytest.mark.parametrize("w,h,n,field,removal,masked,ssim", [
     (64, 64, 400, "random", False, False, 0.0), (97, 61, 900, "random", True, False, 0.0),
     (128, 128, 2000, "knn", True, True, 0.0), (72, 40, 300, "knn", False, False, 0.2),
-    (96, 80, 6000, "knn", False, False, 0.0)])
+    (96, 80, 6000, "knn", False, False, 0.0), (128, 128, 200, "knn", True, True, 0.0),
+    (160, 96, 150, "knn", False, False, 0.2), (99, 70, 120, "knn", True, False, 0.0)])
 def test_trainer_gradients_match_oracle(ops, orc, w, h, n, field, removal, masked, ssim):
     """The trainer's kernel (precomputed tile registration, sites staged in shared memory,
     fixed-point sums) against the oracle and against the float API kernel on the same
     inputs.  The random fields put far more than a tile table's 256 keys in each 16x16 tile
     (the global path) and repeat ids within lists; the k-nearest fields are what a fit
-    sees, and at 6000 sites on 96x80 they too overflow the tables.  (A random field that
+    sees, and at 6000 sites on 96x80 they too overflow the tables; the sparse k-nearest
+    fields (80-120 pixels per site, the density of the late fit) give every lane of a warp
+    nearly the same list, with masked and partial warps among them.  (A random field that
     dense is not used against the oracle: its far candidates give single-pixel terms of
     ~1e-6 whose FP32 value, identical in both GPU kernels, is ill-conditioned.)  Fixed
     point: the same sums to the last bit on a second run."""
@@ -362,6 +365,33 @@ def test_prune_pipeline_bit_exact(ops, orc):
     s_t = tf(sites)
     ops.prune_sites(s_t, idx, k)
     np.testing.assert_array_equal(s_t.cpu().numpy(), orc.prune_sites(sites, srt[:k, 1]))
+
+
+@pytest.mark.parametrize("n,frac", [(0, 0.5), (1, 0.0), (1, 1.0), (1023, 0.5), (1024, 0.93), (1025, 0.5),
+                                    (128000, 0.93), (70001, 0.0), (70001, 1.0)])
+def test_compact_active_matches_numpy(cuda, n, frac):
+    """Stream compaction of the active sites through the C ABI: the ascending indices with
+    pos_x >= 0 (frac of the sites inactive) and their count, against numpy; integer work,
+    so bit-exact."""
+    import ctypes as C
+    from sad_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(n + int(frac * 100))
+    sites = rng.random((max(n, 1), 10)).astype(np.float32)
+    sites[:n][rng.random(n) < frac, 0] = -1.0
+    want = np.nonzero(sites[:n, 0] >= 0)[0].astype(np.uint32)
+    s_t = tf(sites)
+    alive = torch.full((max(n, 1),), -1, dtype=torch.int32, device="cuda")
+    count = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nb = lib.sad_compact_active_scratch_bytes(n)
+    scratch = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    st = lib.sad_compact_active(C.c_void_p(s_t.data_ptr()), n, C.c_void_p(alive.data_ptr()),
+                                C.c_void_p(count.data_ptr()), C.c_void_p(scratch.data_ptr()), nb, None)
+    assert st == 0, lib.sad_last_error()
+    torch.cuda.synchronize()
+    k = int(count.item())
+    assert k == want.size
+    np.testing.assert_array_equal(u32(alive)[:k], want)
 
 
 def test_densify_pairs_and_split(ops, orc):
