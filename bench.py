@@ -336,7 +336,8 @@ def batch_images(count: int):
 
 
 def run_batch(args):
-    """All images submitted at once to the executor; the step is the whole batch."""
+    """The 64-image batch; the step is the whole batch: by default one lockstep batch
+    (sad_batch_*), or (--batch-mode executor) all images submitted at once to the executor."""
     import torch
     from sad_gb300.config import train_config
     from sad_gb300.executor import Executor
@@ -359,16 +360,38 @@ def run_batch(args):
             res = [r.result() for r in reqs]
         return wall, [p for _, p in res], [len(s) for s, _ in res], [r.run_ms for r in reqs]
 
+    def run_lockstep():
+        """One lockstep batch: every stage one launch over all images (sad_batch_*); timed
+        like the executor path, from the host images' upload to every image's sites and
+        PSNR back on the host."""
+        from sad_gb300.batch import Batch
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with Batch([(i.shape[1], i.shape[0]) for i in imgs], config=cfg) as b:
+            for i, img in enumerate(imgs):
+                b.set_target(i, img)
+            b.init()
+            b.run()
+            b.synchronize()
+            psnr = [b.psnr(i) for i in range(len(imgs))]
+            sites = [len(b.sites(i)) for i in range(len(imgs))]
+        return time.perf_counter() - t0, psnr, sites, [float("nan")] * len(imgs)
+
     with Executor(workers=2) as ex:  # warm-up: kernel loading, pool growth
         for img in imgs[:2]:
             ex.submit_fit(img, config=train_config(log_freq=0, iterations=50))
         ex.wait_all()
+    lockstep = args.batch_mode == "lockstep"
+    if lockstep:  # warm-up of the batched kernels on a short batch of the same images
+        from sad_gb300.batch import fit_batch
+        fit_batch(imgs[:4], log_freq=0, iterations=50)
     with ClockSampler(0) as clk:
         walls = []
         for _ in range(args.steps):
-            wall, psnr, sites, run_ms = run(args.workers)
+            wall, psnr, sites, run_ms = run_lockstep() if lockstep else run(args.workers)
             walls.append(wall)
     seq_wall = run(1)[0] if args.batch_sequential else None
+    exec_wall = run(args.workers)[0] if (lockstep and args.batch_compare) else None
     wall = float(np.median(walls))
     return {
         "metric": BATCH_METRIC, "value": round(wall, 3), "unit": "s", "n_gpus": 1, "steps": args.steps,
@@ -377,11 +400,13 @@ def run_batch(args):
         "data": "synthetic: seeded gradient + blobs + polygons per image, quantised to 8 bits",
         "config": {"workload": f"{len(imgs)} fits, sizes {min(i.shape[1] for i in imgs)}-"
                                f"{max(i.shape[1] for i in imgs)} wide, 1.0 bpp, {args.batch_iters} iterations "
-                               f"each, {args.workers} executor workers",
+                               f"each, " + ("lockstep batch (one launch per stage over all images, graph "
+                                           "replays)" if lockstep else f"{args.workers} executor workers"),
                    "images": [f"{i.shape[1]}x{i.shape[0]}" for i in imgs]},
         "mpix_iters_per_s": round(mpix_iters / wall, 1),
         "images_per_s": round(len(imgs) / wall, 3),
         "sequential_wall_s": None if seq_wall is None else round(seq_wall, 3),
+        "executor_wall_s": None if exec_wall is None else round(exec_wall, 3),
         "psnr_db_mean": round(float(np.mean(psnr)), 3), "sites_final_total": int(sum(sites)),
         "fit_run_ms": {"p50": round(float(np.median(run_ms)), 1), "max": round(float(np.max(run_ms)), 1)},
         "e2e": {"value": round(wall, 3), "unit": "s", "h2d_bytes_per_step": int(sum(i.nbytes for i in imgs)),
@@ -541,6 +566,8 @@ def main():
     ap.add_argument("--batch-images", type=int, default=64)
     ap.add_argument("--batch-iters", type=int, default=2000)
     ap.add_argument("--batch-sequential", action="store_true", help="also time the batch with one worker")
+    ap.add_argument("--batch-mode", default="lockstep", choices=["lockstep", "executor"])
+    ap.add_argument("--batch-compare", action="store_true", help="lockstep: also time the executor path")
     ap.add_argument("--serve-rates", default="5,10,20,40")
     ap.add_argument("--serve-count", type=int, default=120)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)

@@ -441,6 +441,37 @@ sad_status_t sad_trainer_fit_host(sad_trainer_t* t, const float* target_host,
                                   int* written, float* psnr_out);
 
 /* ------------------------------------------------------------------------ */
+/* batched fits: many images in lockstep, one launch per stage               */
+/* ------------------------------------------------------------------------ */
+
+/* A batch of n_images fits with one configuration (sizes may differ): each image owns a
+ * trainer (reachable with sad_batch_trainer for its target, PSNR, render and sites), and
+ * every iteration runs each stage as one launch over all images -- the per-pixel kernels
+ * over a per-image tile work list, the per-site kernels over the images' compacted active
+ * lists walked as one -- replayed as one CUDA graph per iteration kind.  Per image the
+ * result is bitwise that of its own sad_trainer fit.  The schedule must be common: one VPT
+ * pass per refresh, no SSIM loss, and no densify step firing (the default configuration);
+ * sad_batch_init rejects others with SAD_ERR_UNSUPPORTED.  At most 1024 images.
+ * No counterpart in the reference: it fits one image per process (run.sh batch mode,
+ * run.sh:262-373). */
+typedef struct sad_batch sad_batch_t;
+sad_status_t sad_batch_create(const sad_train_config_t* cfg, int n_images, const int* widths,
+                              const int* heights, sad_batch_t** out);
+sad_status_t sad_batch_destroy(sad_batch_t* b);
+/* The trainer of image i (owned by the batch): set its target before sad_batch_init. */
+sad_status_t sad_batch_trainer(sad_batch_t* b, int image, sad_trainer_t** out);
+/* Gradient-weighted init of every image and the batch's launch tables. */
+sad_status_t sad_batch_init(sad_batch_t* b);
+/* Iterations up to `end` (exclusive) of every image, on the batch's stream. */
+sad_status_t sad_batch_run(sad_batch_t* b, int end);
+sad_status_t sad_batch_synchronize(sad_batch_t* b);
+sad_stream_t sad_batch_stream(sad_batch_t* b);
+/* Event-time every batched gradient launch (eager launches while enabled) and report
+ * the mean launch duration of the last sad_batch_run. */
+sad_status_t sad_batch_enable_timing(sad_batch_t* b, int enable);
+sad_status_t sad_batch_gradient_ms(sad_batch_t* b, double* ms_per_launch);
+
+/* ------------------------------------------------------------------------ */
 /* render from sites (serving path)                                          */
 /* ------------------------------------------------------------------------ */
 

@@ -98,6 +98,15 @@ SIGNATURES = {
     "sad_radix_sort_pairs_noalloc": (st, [vp, u32, u32, vp]),
     "sad_write_split_indices": (st, [vp, vp, u32, vp]),
     "sad_prune_sites": (st, [vp, vp, u32, vp]),
+    "sad_batch_create": (st, [C.POINTER(TrainConfig), i32, vp, vp, vp]),
+    "sad_batch_destroy": (st, [vp]),
+    "sad_batch_trainer": (st, [vp, i32, vp]),
+    "sad_batch_init": (st, [vp]),
+    "sad_batch_run": (st, [vp, i32]),
+    "sad_batch_synchronize": (st, [vp]),
+    "sad_batch_stream": (vp, [vp]),
+    "sad_batch_enable_timing": (st, [vp, i32]),
+    "sad_batch_gradient_ms": (st, [vp, vp]),
     "sad_compact_active_scratch_bytes": (sz, [u32]),
     "sad_compact_active": (st, [vp, u32, vp, vp, vp, sz, vp]),
     "sad_split_sites": (st, [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp, vp, u32, vp, i32, i32, vp]),

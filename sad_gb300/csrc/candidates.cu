@@ -112,6 +112,26 @@ void launch_pack_geom(const Site* sites, SiteGeom* out, uint32_t n, cudaStream_t
     note_launches(1);
 }
 
+__global__ void __launch_bounds__(256) pack_geom_batch_kernel(const SiteBatchItem* __restrict__ items,
+                                                              const uint32_t* __restrict__ prefix,
+                                                              uint32_t n_items) {
+    pdl_wait();
+    __shared__ uint32_t s_prefix[kMaxBatchItems + 1];
+    const uint32_t total = load_site_prefix(s_prefix, prefix, n_items);
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const uint32_t k = batch_item_of(s_prefix, n_items, g);
+        const SiteBatchItem& it = items[k];
+        pack_geom_one(it.sites, it.vgeom, it.alive[g - s_prefix[k]]);
+    }
+}
+
+void launch_pack_geom_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items,
+                            uint32_t grid_threads, cudaStream_t st) {
+    launch_pdl(pack_geom_batch_kernel, dim3(std::max(1u, blocks_for(grid_threads, 256))), dim3(256), 0, st, items,
+               site_prefix, n_items);
+    note_launches(1);
+}
+
 void launch_pack_geom_alive(const Site* sites, SiteGeom* out, const uint32_t* alive, const DevState* state,
                             uint32_t max_alive, cudaStream_t st) {
     if (max_alive == 0) return;
@@ -292,6 +312,43 @@ __global__ void __launch_bounds__(256, 5) vpt_kernel(VptParams prm, Src src) {
     if (x >= prm.width || y >= prm.height) return;
     uint32_t out[8];
     vpt_pixel(prm, src, x, y, out);
+}
+
+// Batched form over the 32x8-pixel blocks of every image of a batch (the trainer's
+// refresh pass on the f16-rounded geometry).
+__global__ void __launch_bounds__(256, 5) vpt_batch_kernel(const VptBatchItem* __restrict__ items,
+                                                           const uint32_t* __restrict__ block_prefix,
+                                                           uint32_t n_items) {
+    pdl_wait();
+    __shared__ VptParams s_p;
+    __shared__ const SiteGeom* s_g;
+    __shared__ int s_local, s_bx;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    if (tid == 0) {
+        uint32_t lo = 0, hi = n_items;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(block_prefix + mid) <= blockIdx.x) lo = mid;
+            else hi = mid;
+        }
+        s_p = items[lo].p;
+        s_g = items[lo].vgeom;
+        s_bx = items[lo].blocks_x;
+        s_local = static_cast<int>(blockIdx.x - block_prefix[lo]);
+    }
+    __syncthreads();
+    const int x = (s_local % s_bx) * 32 + threadIdx.x;
+    const int y = (s_local / s_bx) * 8 + threadIdx.y;
+    if (x >= s_p.width || y >= s_p.height) return;
+    uint32_t out[8];
+    vpt_pixel(s_p, PackedGeomSites{s_g}, x, y, out);
+}
+
+void launch_vpt_batch(const VptBatchItem* items, const uint32_t* block_prefix, uint32_t n_items,
+                      uint32_t total_blocks, cudaStream_t st) {
+    if (total_blocks == 0) return;
+    launch_pdl(vpt_batch_kernel, dim3(total_blocks), dim3(32, 8), 0, st, items, block_prefix, n_items);
+    note_launches(1);
 }
 
 static dim3 pixel_grid(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }

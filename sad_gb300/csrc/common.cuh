@@ -163,6 +163,30 @@ __device__ __forceinline__ float dmix2(const SiteGeom& g, float ux, float uy, fl
     return sqrtf(m.d2_safe) - g.radius * inv_scale;
 }
 
+// Item of flat index g in a batch walked as one list: prefix (shared or global) holds the
+// first flat index of each of the n_items items and prefix[n_items] the total.
+__device__ __forceinline__ uint32_t batch_item_of(const uint32_t* prefix, uint32_t n_items, uint32_t g) {
+    uint32_t lo = 0, hi = n_items;  // prefix[lo] <= g < prefix[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (prefix[mid] <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Largest batch of images a batched launch serves (its flat-list prefix is staged in
+// shared memory).
+constexpr uint32_t kMaxBatchItems = 1024;
+
+// Loads a flat-list prefix (n_items + 1 words) into shared memory; returns the total.
+__device__ __forceinline__ uint32_t load_site_prefix(uint32_t* s_prefix, const uint32_t* __restrict__ prefix,
+                                                     uint32_t n_items) {
+    for (uint32_t k = threadIdx.x; k <= n_items; k += blockDim.x) s_prefix[k] = prefix[k];
+    __syncthreads();
+    return s_prefix[n_items];
+}
+
 __device__ __forceinline__ uint32_t lane_id() {
     uint32_t l;
     asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));

@@ -340,13 +340,55 @@ __global__ void __launch_bounds__(256, 3) fused_gradients_kernel(GradParams prm,
 // reads each candidate's table index, weight and site data by index instead of carrying
 // rotated register arrays.
 template <class Src, bool kRemoval, bool kSSIM>
+__device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& src, int bx, int by, int tiles_x);
+
+template <class Src, bool kRemoval, bool kSSIM>
 __global__ void __launch_bounds__(256, 4) fused_gradients_pre_kernel(GradParams prm, Src src) {
     pdl_wait();
+    grad_pre_tile<Src, kRemoval, kSSIM>(prm, src, blockIdx.x, blockIdx.y, gridDim.x);
+}
+
+// Image of a batched launch's block: the last item whose first block is <= b (prefix[0]
+// = 0 and prefix[n_items] = the grid's block count).
+__device__ __forceinline__ uint32_t batch_item_of_block(const uint32_t* __restrict__ prefix, uint32_t items,
+                                                        uint32_t b) {
+    uint32_t lo = 0, hi = items;  // prefix[lo] <= b < prefix[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(prefix + mid) <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Batched form: one launch over the tiles of every image of a batch (tile_prefix[i] is the
+// first block of image i); each block copies its image's parameters into shared memory.
+template <class Src, bool kRemoval, bool kSSIM>
+__global__ void __launch_bounds__(256, 4) fused_gradients_batch_kernel(const GradBatchItem* __restrict__ items,
+                                                                       const uint32_t* __restrict__ tile_prefix,
+                                                                       uint32_t n_items) {
+    pdl_wait();
+    __shared__ GradParams s_prm;
+    __shared__ Src s_src;
+    __shared__ int s_local, s_tiles_x;
+    if (threadIdx.x == 0) {
+        const uint32_t i = batch_item_of_block(tile_prefix, n_items, blockIdx.x);
+        s_prm = items[i].p;
+        s_src = Src{items[i].geom, items[i].color};
+        s_tiles_x = items[i].tiles_x;
+        s_local = static_cast<int>(blockIdx.x - tile_prefix[i]);
+    }
+    __syncthreads();
+    grad_pre_tile<Src, kRemoval, kSSIM>(s_prm, s_src, s_local % s_tiles_x, s_local / s_tiles_x, s_tiles_x);
+}
+
+template <class Src, bool kRemoval, bool kSSIM>
+__device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& src, int bx, int by, int tiles_x) {
     using L = GradLayout<true, kRemoval>;
     constexpr int NV = L::NV;
     auto& sm = shared_table<typename L::Pre>();
     const int tid = threadIdx.x;
-    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int tile = by * tiles_x + bx;
     const int used = prm.tile_count[tile];
     {
         const uint32_t* keys = prm.tile_keys + static_cast<size_t>(tile) * kTileKeys;
@@ -365,8 +407,8 @@ __global__ void __launch_bounds__(256, 4) fused_gradients_pre_kernel(GradParams 
     __syncthreads();
 
     const int lane = tid & 31, warp = tid >> 5;
-    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
-    const int y = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+    const int x = bx * 16 + (warp & 1) * 8 + (lane & 7);
+    const int y = by * 16 + (warp >> 1) * 4 + (lane >> 3);
     const int w = prm.width, h = prm.height;
     const float inv_s2 = prm.inv_scale_sq;
     const float inv_scale = sqrtf(inv_s2);
@@ -452,17 +494,45 @@ __global__ void __launch_bounds__(256, 4) fused_gradients_pre_kernel(GradParams 
 // and each tile's key list, with the gradient kernel's tiling (16x16 tiles, 8x4 warp
 // patches) and its registration (one CAS per warp and site).  Every candidate id below
 // n is registered; inactive sites simply receive no value.
+__device__ __forceinline__ void register_tile(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
+                                              uint32_t n, int w, int h, int cw, int ch, const TileMap& map,
+                                              int bx, int by, int tiles_x);
+
 __global__ void __launch_bounds__(256) register_tiles_kernel(const uint4* __restrict__ c0,
                                                              const uint4* __restrict__ c1, uint32_t n,
                                                              int w, int h, int cw, int ch, TileMap map) {
     pdl_wait();
+    register_tile(c0, c1, n, w, h, cw, ch, map, blockIdx.x, blockIdx.y, gridDim.x);
+}
+
+// Batched form over the tiles of every image of a batch.
+__global__ void __launch_bounds__(256) register_tiles_batch_kernel(const RegisterBatchItem* __restrict__ items,
+                                                                   const uint32_t* __restrict__ tile_prefix,
+                                                                   uint32_t n_items) {
+    pdl_wait();
+    __shared__ RegisterBatchItem s_it;
+    __shared__ int s_local;
+    if (threadIdx.x == 0) {
+        const uint32_t i = batch_item_of_block(tile_prefix, n_items, blockIdx.x);
+        s_it = items[i];
+        s_local = static_cast<int>(blockIdx.x - tile_prefix[i]);
+    }
+    __syncthreads();
+    const int tx = s_it.tiles_x;
+    register_tile(reinterpret_cast<const uint4*>(s_it.c0), reinterpret_cast<const uint4*>(s_it.c1), s_it.n, s_it.w,
+                  s_it.h, s_it.cw, s_it.ch, s_it.map, s_local % tx, s_local / tx, tx);
+}
+
+__device__ __forceinline__ void register_tile(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
+                                              uint32_t n, int w, int h, int cw, int ch, const TileMap& map,
+                                              int bx, int by, int tiles_x) {
     __shared__ KeyTable<512> table;
     const int tid = threadIdx.x;
     table.init_keys(tid, 256);
     __syncthreads();
     const int lane = tid & 31, warp = tid >> 5;
-    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
-    const int y = blockIdx.y * 16 + (warp >> 1) * 4 + (lane >> 3);
+    const int x = bx * 16 + (warp & 1) * 8 + (lane & 7);
+    const int y = by * 16 + (warp >> 1) * 4 + (lane >> 3);
     const bool inside = x < w && y < h;
     uint32_t ids[kCand];
     if (inside) {
@@ -476,7 +546,7 @@ __global__ void __launch_bounds__(256) register_tiles_kernel(const uint4* __rest
     }
     register_tile_pixel(table, ids, n, x, y, w, inside, map);
     __syncthreads();
-    write_tile_keys(table, tid, blockIdx.y * gridDim.x + blockIdx.x, map);
+    write_tile_keys(table, tid, by * tiles_x + bx, map);
 }
 
 size_t tile_map_words(int w, int h) {
@@ -498,6 +568,13 @@ void launch_register_tiles(const uint32_t* c0, const uint32_t* c1, uint32_t n, i
     dim3 grid((w + 15) / 16, (h + 15) / 16);
     launch_pdl(register_tiles_kernel, grid, dim3(256), 0, st, reinterpret_cast<const uint4*>(c0),
                reinterpret_cast<const uint4*>(c1), n, w, h, cw, ch, map);
+    note_launches(1);
+}
+
+void launch_register_tiles_batch(const RegisterBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
+                                 uint32_t total_tiles, cudaStream_t st) {
+    if (total_tiles == 0) return;
+    launch_pdl(register_tiles_batch_kernel, dim3(total_tiles), dim3(256), 0, st, items, tile_prefix, n_items);
     note_launches(1);
 }
 
@@ -553,6 +630,10 @@ static cudaError_t allow_variant() {
         size_t pre = sizeof(typename GradLayout<true, kRemoval>::Pre);
         if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_pre_kernel<Src, kRemoval, false>, pre);
         if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_pre_kernel<Src, kRemoval, true>, pre);
+        if constexpr (std::is_same<Src, PreparedSites>::value) {
+            if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_batch_kernel<Src, kRemoval, false>, pre);
+            if (e == cudaSuccess) e = allow_dynamic_smem(fused_gradients_batch_kernel<Src, kRemoval, true>, pre);
+        }
     }
     return e;
 }
@@ -575,6 +656,28 @@ void launch_gradients_prepared(const GradParams& p, const SiteGeom* geom, const 
         dispatch_gradients<PreparedSites, true>(p, PreparedSites{geom, color}, st);
     else
         dispatch_gradients<PreparedSites, false>(p, PreparedSites{geom, color}, st);
+}
+
+template <bool kRemoval, bool kSSIM>
+static void launch_batch_variant(const GradBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
+                                 uint32_t total_tiles, cudaStream_t st) {
+    launch_pdl(fused_gradients_batch_kernel<PreparedSites, kRemoval, kSSIM>, dim3(total_tiles), dim3(256),
+               sizeof(typename GradLayout<true, kRemoval>::Pre), st, items, tile_prefix, n_items);
+}
+
+void launch_gradients_batch(const GradBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
+                            uint32_t total_tiles, bool removal, bool ssim, cudaStream_t st) {
+    if (total_tiles == 0) return;
+    ensure_gradient_kernels();
+    if (removal && ssim)
+        launch_batch_variant<true, true>(items, tile_prefix, n_items, total_tiles, st);
+    else if (removal)
+        launch_batch_variant<true, false>(items, tile_prefix, n_items, total_tiles, st);
+    else if (ssim)
+        launch_batch_variant<false, true>(items, tile_prefix, n_items, total_tiles, st);
+    else
+        launch_batch_variant<false, false>(items, tile_prefix, n_items, total_tiles, st);
+    note_launches(1);
 }
 
 }  // namespace sad

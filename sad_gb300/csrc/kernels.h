@@ -36,6 +36,16 @@ struct VptParams {
     uint32_t pow2, stages;
 };
 
+// Batched VPT pass: one grid over the 32x8 blocks of every image (block_prefix[i] is image
+// i's first block); items and prefix in device memory.
+struct VptBatchItem {
+    VptParams p;
+    const SiteGeom* vgeom;
+    int blocks_x;
+};
+void launch_vpt_batch(const VptBatchItem* items, const uint32_t* block_prefix, uint32_t n_items,
+                      uint32_t total_blocks, cudaStream_t st);
+
 // render.cu
 void launch_prepare_sites(const Site* sites, SiteGeom* geom, SiteColor* color, uint32_t n,
                           cudaStream_t st);
@@ -106,6 +116,27 @@ struct TileMap {
     uint32_t* tile_keys;
     int* tile_count;
 };
+// Batched launches: one grid over the tiles of every image of a batch; tile_prefix[i] is
+// image i's first block (tile_prefix[n_items] = total_tiles); items and prefixes live in
+// device memory.
+struct GradBatchItem {
+    GradParams p;
+    const SiteGeom* geom;
+    const SiteColor* color;
+    int tiles_x;
+};
+struct RegisterBatchItem {
+    const uint32_t* c0;
+    const uint32_t* c1;
+    uint32_t n;
+    int w, h, cw, ch;
+    TileMap map;
+    int tiles_x;
+};
+void launch_gradients_batch(const GradBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
+                            uint32_t total_tiles, bool removal, bool ssim, cudaStream_t st);
+void launch_register_tiles_batch(const RegisterBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
+                                 uint32_t total_tiles, cudaStream_t st);
 size_t tile_map_words(int w, int h);  // u32 words of one TileMap (slot map + keys + counts)
 TileMap tile_map_at(uint32_t* base, int w, int h);
 void launch_register_tiles(const uint32_t* c0, const uint32_t* c1, uint32_t n, int w, int h,
@@ -145,6 +176,50 @@ void launch_adam_train(Site* sites, float* adam, long long* fix12, const uint32_
                        SiteGeom* geom, SiteColor* color, const AdamHyper& hp,
                        const DevState* state, int iterations, uint32_t max_alive, int w, int h,
                        cudaStream_t st);
+// Batched per-site launches over the compacted active lists of every image of a batch,
+// walked as one flat list: site_prefix[i] = sum of the n_alive of images < i (in device
+// memory, written by launch_batch_site_prefix after each compaction); grid-stride, so the
+// grid size is only a size hint.  items in device memory.
+struct SiteBatchItem {
+    Site* sites;
+    SiteGeom* geom;
+    SiteColor* color;
+    SiteGeom* vgeom;
+    float* adam;
+    long long* grads;
+    float* tau_a;
+    float* tau_b;
+    uint32_t* tau_nbr;
+    float* tau_raw;
+    uint32_t* alive;
+    uint32_t* alive_blocks;
+    DevState* state;
+    const uint32_t* cand0[3];
+    const uint32_t* cand1[3];
+    uint32_t* pairs;
+    const uint32_t* prune_k;
+    uint32_t n;  // buffer site count
+    int w, h, cw, ch, ds;
+    float removal_inv_mul;  // 1 / the removal pre-scale of the gradient records
+    float delta_norm;
+};
+void launch_batch_site_prefix(const SiteBatchItem* items, uint32_t n_items, uint32_t* site_prefix, cudaStream_t st);
+void launch_tau_first_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items, int field,
+                            int iterations, uint32_t grid_threads, cudaStream_t st);
+// a_to_b: tau_a -> tau_b, else tau_b -> tau_a
+void launch_tau_list_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items, bool a_to_b,
+                           int iterations, uint32_t grid_threads, cudaStream_t st);
+void launch_adam_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items,
+                       const AdamHyper& hp, int iterations, uint32_t grid_threads, cudaStream_t st);
+void launch_advance_state_batch(const SiteBatchItem* items, uint32_t n_items, uint32_t vpt_passes, float beta1,
+                                float beta2, cudaStream_t st);
+void launch_pack_geom_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items,
+                            uint32_t grid_threads, cudaStream_t st);
+void launch_prune_pairs_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items,
+                              uint32_t grid_threads, cudaStream_t st);
+void launch_prune_sorted_batch(const SiteBatchItem* items, uint32_t n_items, uint32_t max_k, cudaStream_t st);
+// compaction of every image's [0, n) (max_blocks = the largest compact_blocks(n) of the batch)
+void launch_compact_batch(const SiteBatchItem* items, uint32_t n_items, uint32_t max_blocks, cudaStream_t st);
 void launch_clear_f32(float* buf, size_t count, cudaStream_t st);
 // iteration counter, VPT pass counter and the next iteration's Adam bias corrections
 void launch_reset_state(DevState* state, float beta1, float beta2, cudaStream_t st);

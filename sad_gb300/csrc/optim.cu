@@ -465,6 +465,116 @@ void launch_advance_state(DevState* state, uint32_t vpt_passes, float beta1, flo
     note_launches(1);
 }
 
+// ---------------------------------------------------------------------------
+// batched forms: every image of a batch in one launch, over the flat active list
+// ---------------------------------------------------------------------------
+__global__ void batch_site_prefix_kernel(const SiteBatchItem* __restrict__ items, uint32_t n_items,
+                                         uint32_t* __restrict__ prefix) {
+    pdl_wait();
+    if (threadIdx.x != 0) return;
+    uint32_t run = 0;
+    for (uint32_t i = 0; i < n_items; ++i) {
+        prefix[i] = run;
+        run += items[i].state->n_alive;
+    }
+    prefix[n_items] = run;
+}
+
+void launch_batch_site_prefix(const SiteBatchItem* items, uint32_t n_items, uint32_t* site_prefix, cudaStream_t st) {
+    launch_pdl(batch_site_prefix_kernel, dim3(1), dim3(32), 0, st, items, n_items, site_prefix);
+    note_launches(1);
+}
+
+__global__ void __launch_bounds__(256) tau_first_batch_kernel(const SiteBatchItem* __restrict__ items,
+                                                              const uint32_t* __restrict__ prefix,
+                                                              uint32_t n_items, int field, int iterations) {
+    pdl_wait();
+    __shared__ uint32_t s_prefix[kMaxBatchItems + 1];
+    const uint32_t total = load_site_prefix(s_prefix, prefix, n_items);
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const uint32_t k = batch_item_of(s_prefix, n_items, g);
+        const SiteBatchItem& it = items[k];
+        TauLists tl{reinterpret_cast<uint4*>(it.tau_nbr), it.tau_raw, it.alive};
+        const uint32_t i = it.alive[g - s_prefix[k]];
+        tau_first_one(reinterpret_cast<const uint4*>(it.cand0[field]), reinterpret_cast<const uint4*>(it.cand1[field]),
+                      it.geom, it.grads, tl, it.tau_a, it.n, i, tau_lambda(it.state->iter, iterations), it.cw,
+                      it.ch, it.ds);
+    }
+}
+
+__global__ void __launch_bounds__(256) tau_list_batch_kernel(const SiteBatchItem* __restrict__ items,
+                                                             const uint32_t* __restrict__ prefix,
+                                                             uint32_t n_items, int a_to_b, int iterations) {
+    pdl_wait();
+    __shared__ uint32_t s_prefix[kMaxBatchItems + 1];
+    const uint32_t total = load_site_prefix(s_prefix, prefix, n_items);
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const uint32_t k = batch_item_of(s_prefix, n_items, g);
+        const SiteBatchItem& it = items[k];
+        TauLists tl{reinterpret_cast<uint4*>(it.tau_nbr), it.tau_raw, it.alive};
+        const uint32_t i = it.alive[g - s_prefix[k]];
+        const float* gin = a_to_b ? it.tau_a : it.tau_b;
+        float* gout = a_to_b ? it.tau_b : it.tau_a;
+        gout[i] = tau_list_pass(tl, gin, i, tau_lambda(it.state->iter, iterations));
+    }
+}
+
+__global__ void __launch_bounds__(256) adam_batch_kernel(const SiteBatchItem* __restrict__ items,
+                                                         const uint32_t* __restrict__ prefix, uint32_t n_items,
+                                                         AdamHyper hp, int iterations) {
+    pdl_wait();
+    __shared__ uint32_t s_prefix[kMaxBatchItems + 1];
+    const uint32_t total = load_site_prefix(s_prefix, prefix, n_items);
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const uint32_t k = batch_item_of(s_prefix, n_items, g);
+        const SiteBatchItem& it = items[k];
+        TauLists tl{reinterpret_cast<uint4*>(it.tau_nbr), it.tau_raw, it.alive};
+        adam_train_one(it.sites, it.adam, it.grads, tl, it.tau_a, it.geom, it.color, hp, it.state, iterations, it.w,
+                       it.h, it.alive[g - s_prefix[k]]);
+    }
+}
+
+__global__ void advance_state_batch_kernel(const SiteBatchItem* __restrict__ items, uint32_t n_items,
+                                           uint32_t vpt_passes, float beta1, float beta2) {
+    pdl_wait();
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_items) return;
+    DevState* state = items[k].state;
+    state->iter += 1u;
+    state->vpt_pass += vpt_passes;
+    set_bias_corrections(state, beta1, beta2);
+}
+
+static unsigned batch_grid(uint32_t grid_threads) { return std::max(1u, blocks_for(grid_threads, 256)); }
+
+void launch_tau_first_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items, int field,
+                            int iterations, uint32_t grid_threads, cudaStream_t st) {
+    launch_pdl(tau_first_batch_kernel, dim3(batch_grid(grid_threads)), dim3(256), 0, st, items, site_prefix, n_items,
+               field, iterations);
+    note_launches(1);
+}
+
+void launch_tau_list_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items, bool a_to_b,
+                           int iterations, uint32_t grid_threads, cudaStream_t st) {
+    launch_pdl(tau_list_batch_kernel, dim3(batch_grid(grid_threads)), dim3(256), 0, st, items, site_prefix, n_items,
+               a_to_b ? 1 : 0, iterations);
+    note_launches(1);
+}
+
+void launch_adam_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items,
+                       const AdamHyper& hp, int iterations, uint32_t grid_threads, cudaStream_t st) {
+    launch_pdl(adam_batch_kernel, dim3(batch_grid(grid_threads)), dim3(256), 0, st, items, site_prefix, n_items, hp,
+               iterations);
+    note_launches(1);
+}
+
+void launch_advance_state_batch(const SiteBatchItem* items, uint32_t n_items, uint32_t vpt_passes, float beta1,
+                                float beta2, cudaStream_t st) {
+    launch_pdl(advance_state_batch_kernel, dim3(blocks_for(n_items, 128)), dim3(128), 0, st, items, n_items,
+               vpt_passes, beta1, beta2);
+    note_launches(1);
+}
+
 }  // namespace sad
 
 using namespace sad;

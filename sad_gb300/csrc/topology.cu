@@ -110,6 +110,34 @@ __global__ void prune_pairs_alive_kernel(long long* __restrict__ fix12, float in
     }
 }
 
+__global__ void __launch_bounds__(256) prune_pairs_batch_kernel(const SiteBatchItem* __restrict__ items,
+                                                                const uint32_t* __restrict__ prefix,
+                                                                uint32_t n_items) {
+    pdl_wait();
+    __shared__ uint32_t s_prefix[kMaxBatchItems + 1];
+    const uint32_t total = load_site_prefix(s_prefix, prefix, n_items);
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const uint32_t k = batch_item_of(s_prefix, n_items, g);
+        const SiteBatchItem& it = items[k];
+        const uint32_t j = g - s_prefix[k];
+        const uint32_t i = it.alive[j];
+        longlong2* r = reinterpret_cast<longlong2*>(it.grads + static_cast<size_t>(i) * 12 + 10);
+        longlong2 v = *r;
+        *r = make_longlong2(0, 0);
+        float removal = static_cast<float>(v.y) * 1.0e6f + from_fix(v.x) * it.removal_inv_mul;
+        float delta = removal * it.delta_norm;
+        reinterpret_cast<uint2*>(it.pairs)[j] = isfinite(delta) ? make_uint2(__float_as_uint(fmaxf(delta, 0.0f)), i)
+                                                                : make_uint2(kEmpty, kEmpty);
+    }
+}
+
+void launch_prune_pairs_batch(const SiteBatchItem* items, const uint32_t* site_prefix, uint32_t n_items,
+                              uint32_t grid_threads, cudaStream_t st) {
+    launch_pdl(prune_pairs_batch_kernel, dim3(std::max(1u, blocks_for(grid_threads, 256))), dim3(256), 0, st, items,
+               site_prefix, n_items);
+    note_launches(1);
+}
+
 void launch_prune_pairs_alive(long long* fix12, float fix_mul, uint32_t* pairs, const uint32_t* alive,
                               const DevState* state, uint32_t max_alive, float delta_norm, cudaStream_t st) {
     if (max_alive == 0) return;
@@ -175,6 +203,29 @@ __global__ void prune_sorted_kernel(Site* __restrict__ sites, SiteGeom* __restri
     geom[s].py = -1.0f;
     vgeom[s].px = -1.0f;
     vgeom[s].py = -1.0f;
+}
+
+// Batched form: blockIdx.y is the image; each marks the first prune_k[iter] of its pairs.
+__global__ void prune_sorted_batch_kernel(const SiteBatchItem* __restrict__ items) {
+    pdl_wait();
+    const SiteBatchItem& it = items[blockIdx.y];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t k = it.prune_k[it.state->iter];
+    if (i >= k) return;
+    const uint32_t s = reinterpret_cast<const uint2*>(it.pairs)[i].y;
+    if (s == kEmpty) return;
+    it.sites[s].px = -1.0f;
+    it.sites[s].py = -1.0f;
+    it.geom[s].px = -1.0f;
+    it.geom[s].py = -1.0f;
+    it.vgeom[s].px = -1.0f;
+    it.vgeom[s].py = -1.0f;
+}
+
+void launch_prune_sorted_batch(const SiteBatchItem* items, uint32_t n_items, uint32_t max_k, cudaStream_t st) {
+    if (max_k == 0 || n_items == 0) return;
+    launch_pdl(prune_sorted_batch_kernel, dim3(blocks_for(max_k, 256), n_items), dim3(256), 0, st, items);
+    note_launches(1);
 }
 
 void launch_prune_sorted_train(Site* sites, SiteGeom* geom, SiteGeom* vgeom, const uint32_t* pairs,
@@ -690,6 +741,7 @@ constexpr int kCompactPer = 4;  // sites per thread
 constexpr int kCompactBlock = kCompactThreads * kCompactPer;
 
 uint32_t compact_blocks(uint32_t n) { return (n + kCompactBlock - 1) / kCompactBlock; }
+__device__ __forceinline__ uint32_t compact_blocks_dev(uint32_t n) { return (n + kCompactBlock - 1) / kCompactBlock; }
 
 // Active flags of sites base .. base+3: px[i * stride] >= 0 (stride in floats: 8 for the
 // prepared geometry, 10 for site records).
@@ -704,12 +756,11 @@ __device__ __forceinline__ uint32_t compact_flags(const float* __restrict__ px, 
     return f;
 }
 
-__global__ void __launch_bounds__(kCompactThreads) compact_count_kernel(const float* __restrict__ px,
-                                                                        uint32_t stride, uint32_t n,
-                                                                        uint32_t* __restrict__ counts) {
-    pdl_wait();
+// Active count of compaction block b into counts[b].
+__device__ __forceinline__ void compact_count_block(const float* __restrict__ px, uint32_t stride, uint32_t n,
+                                                    uint32_t* __restrict__ counts, uint32_t b) {
     __shared__ uint32_t warp_sums[kCompactThreads / 32];
-    const uint32_t base = blockIdx.x * kCompactBlock + threadIdx.x * kCompactPer;
+    const uint32_t base = b * kCompactBlock + threadIdx.x * kCompactPer;
     uint32_t c = __popc(compact_flags(px, stride, n, base));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
@@ -719,25 +770,29 @@ __global__ void __launch_bounds__(kCompactThreads) compact_count_kernel(const fl
         uint32_t t = 0;
 #pragma unroll
         for (int w = 0; w < kCompactThreads / 32; ++w) t += warp_sums[w];
-        counts[blockIdx.x] = t;
+        counts[b] = t;
     }
 }
 
-// Each block sums the counts of the blocks before it (a few hundred words even at a
-// million sites), scans its own flags and writes its slots in order; the last block also
-// writes the total.
-__global__ void __launch_bounds__(kCompactThreads) compact_write_kernel(const float* __restrict__ px,
+__global__ void __launch_bounds__(kCompactThreads) compact_count_kernel(const float* __restrict__ px,
                                                                         uint32_t stride, uint32_t n,
-                                                                        const uint32_t* __restrict__ counts,
-                                                                        uint32_t* __restrict__ alive,
-                                                                        uint32_t* __restrict__ n_alive) {
+                                                                        uint32_t* __restrict__ counts) {
     pdl_wait();
+    compact_count_block(px, stride, n, counts, blockIdx.x);
+}
+
+// Compaction block blk of nb: sums the counts of the blocks before it (a few hundred
+// words even at a million sites), scans its own flags and writes its slots in order; the
+// last block also writes the total.
+__device__ __forceinline__ void compact_write_block(const float* __restrict__ px, uint32_t stride, uint32_t n,
+                                                    const uint32_t* __restrict__ counts, uint32_t* __restrict__ alive,
+                                                    uint32_t* __restrict__ n_alive, uint32_t blk, uint32_t nb) {
     __shared__ uint32_t warp_sums[kCompactThreads / 32];
     __shared__ uint32_t s_before;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     {
         uint32_t b = 0;
-        for (uint32_t k = tid; k < blockIdx.x; k += kCompactThreads) b += counts[k];
+        for (uint32_t k = tid; k < blk; k += kCompactThreads) b += counts[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) b += __shfl_down_sync(0xffffffffu, b, o);
         if (lane == 0) warp_sums[warp] = b;
@@ -747,11 +802,11 @@ __global__ void __launch_bounds__(kCompactThreads) compact_write_kernel(const fl
 #pragma unroll
             for (int w = 0; w < kCompactThreads / 32; ++w) t += warp_sums[w];
             s_before = t;
-            if (blockIdx.x == gridDim.x - 1) *n_alive = t + counts[blockIdx.x];
+            if (blk == nb - 1) *n_alive = t + counts[blk];
         }
         __syncthreads();
     }
-    const uint32_t base = blockIdx.x * kCompactBlock + tid * kCompactPer;
+    const uint32_t base = blk * kCompactBlock + tid * kCompactPer;
     const uint32_t f = compact_flags(px, stride, n, base);
     const uint32_t c = __popc(f);
     uint32_t x = c;  // inclusive scan over the warp
@@ -770,6 +825,41 @@ __global__ void __launch_bounds__(kCompactThreads) compact_write_kernel(const fl
 #pragma unroll
     for (int k = 0; k < kCompactPer; ++k)
         if (f >> k & 1u) alive[out++] = base + k;
+}
+
+__global__ void __launch_bounds__(kCompactThreads) compact_write_kernel(const float* __restrict__ px,
+                                                                        uint32_t stride, uint32_t n,
+                                                                        const uint32_t* __restrict__ counts,
+                                                                        uint32_t* __restrict__ alive,
+                                                                        uint32_t* __restrict__ n_alive) {
+    pdl_wait();
+    compact_write_block(px, stride, n, counts, alive, n_alive, blockIdx.x, gridDim.x);
+}
+
+// Batched compaction: blockIdx.y is the image (its prepared geometry over [0, n)); blocks
+// beyond an image's own number of compaction blocks return at once.
+__global__ void __launch_bounds__(kCompactThreads) compact_count_batch_kernel(const SiteBatchItem* __restrict__ items) {
+    pdl_wait();
+    const SiteBatchItem& it = items[blockIdx.y];
+    if (blockIdx.x >= max(1u, compact_blocks_dev(it.n))) return;
+    compact_count_block(reinterpret_cast<const float*>(it.geom), 8u, it.n, it.alive_blocks, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kCompactThreads) compact_write_batch_kernel(const SiteBatchItem* __restrict__ items) {
+    pdl_wait();
+    const SiteBatchItem& it = items[blockIdx.y];
+    const uint32_t nb = max(1u, compact_blocks_dev(it.n));
+    if (blockIdx.x >= nb) return;
+    compact_write_block(reinterpret_cast<const float*>(it.geom), 8u, it.n, it.alive_blocks, it.alive,
+                        &it.state->n_alive, blockIdx.x, nb);
+}
+
+void launch_compact_batch(const SiteBatchItem* items, uint32_t n_items, uint32_t max_blocks, cudaStream_t st) {
+    if (n_items == 0) return;
+    const dim3 grid(std::max(1u, max_blocks), n_items);
+    launch_pdl(compact_count_batch_kernel, grid, dim3(kCompactThreads), 0, st, items);
+    launch_pdl(compact_write_batch_kernel, grid, dim3(kCompactThreads), 0, st, items);
+    note_launches(2);
 }
 
 static void launch_compact(const float* px, uint32_t stride, uint32_t n, uint32_t* block_counts,
