@@ -75,7 +75,10 @@ __device__ __forceinline__ void global_add(const GradParams& p, uint32_t key, co
     if constexpr (kFix) {
         long long* o = p.fix12 + static_cast<size_t>(key) * 12;
 #pragma unroll
-        for (int k = 0; k < NV; ++k) fix_add_global(o + k, to_fix(v[k]));
+        for (int k = 0; k < NV; ++k) {
+            const long long x = to_fix(v[k]);
+            if (x != 0) fix_add_global(o + k, x);  // a zero word leaves the sum as it is
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < 10; ++k) atomicAdd(p.soa[k] + key, v[k]);
@@ -471,6 +474,13 @@ __device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& 
     for (int j = 0; j < kCand; ++j) {
         const int c = static_cast<int>((j + r) & 7u);
         if (!(valid >> c & 1u)) continue;
+        const float wt = sm.wts[c][tid];
+        const float rv = kRemoval ? sm.rem[kRemoval ? c : 0][tid] : 0.0f;
+        // A candidate whose softmax weight underflowed to 0 and that carries no removal
+        // term adds only zero words (every parameter term is a product with its weight):
+        // skipping it leaves every integer sum unchanged.  Far candidates of the random
+        // initial lists are almost all of this kind.
+        if (wt == 0.0f && rv == 0.0f) continue;
         const int slot = slot_of(c);
         uint32_t id = kEmpty;
         if (slot < 0) id = (c < 4 ? prm.cand0 : prm.cand1)[4 * static_cast<size_t>(ci) + (c & 3)];
@@ -478,9 +488,7 @@ __device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& 
         float3 col;
         site_at(id, slot, g, col);
         float v[NV];
-        candidate_values<true, NV>(g, col, ux, uy, inv_s2, inv_scale, sm.wts[c][tid], dLdp, pred,
-                                   kRemoval ? sm.rem[kRemoval ? c : 0][tid] : 0.0f,
-                                   prm.removal_fix_mul, v);
+        candidate_values<true, NV>(g, col, ux, uy, inv_s2, inv_scale, wt, dLdp, pred, rv, prm.removal_fix_mul, v);
         if (slot >= 0)
             sm.vals.add_unique(slot, v, (lane >> 3) & 1);
         else
