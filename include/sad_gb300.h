@@ -584,6 +584,7 @@ typedef struct {
     double queue_ms;    /* submission to start */
     double run_ms;      /* start to results in host memory */
     char message[192];  /* error text when status != SAD_OK */
+    int iteration;      /* fit session: iterations run so far */
 } sad_request_result_t;
 
 typedef struct sad_executor sad_executor_t;
@@ -600,6 +601,29 @@ sad_status_t sad_executor_submit_render(sad_executor_t* ex, const sad_render_con
                                         const float* sites_host, uint32_t site_count, int width,
                                         int height, float* rgb_host, sad_request_result_t* result,
                                         uint64_t* ticket);
+/* Resident fit sessions: a fit whose trainer -- sites, Adam moments, candidate fields and
+ * device counters -- stays on the device between requests.  open_fit queues the session's
+ * start (its slab from the stream-ordered pool, the target uploaded, init; result->psnr is
+ * the initial PSNR) and returns its id; the slab counts against the HBM budget until the
+ * session is closed.  submit_continue queues `iterations` more iterations of the same fit
+ * (stopping at the configuration's total), then copies its active sites (up to capacity)
+ * and PSNR back and reports the iterations run so far in result->iteration.  A session's
+ * requests run one at a time, in submission order, between other requests; a fit
+ * continued in several requests gives the sites of one uninterrupted fit, bit for bit.
+ * close_fit queues the session's end (its slab freed); later requests of it are refused.
+ * Host buffers must stay valid until their request completes.
+ * The reference's nearest behaviour restarts a fit from a sites file
+ * (--init-from-sites, backends/cuda/src/sad_cuda.cu:790-792, 1908-1922), without its Adam
+ * moments. */
+sad_status_t sad_executor_open_fit(sad_executor_t* ex, const sad_train_config_t* cfg,
+                                   const float* target_host, const float* mask_host, int width,
+                                   int height, sad_request_result_t* result, uint64_t* session,
+                                   uint64_t* ticket);
+sad_status_t sad_executor_submit_continue(sad_executor_t* ex, uint64_t session, int iterations,
+                                          float* sites_host, int capacity,
+                                          sad_request_result_t* result, uint64_t* ticket);
+sad_status_t sad_executor_close_fit(sad_executor_t* ex, uint64_t session,
+                                    sad_request_result_t* result, uint64_t* ticket);
 sad_status_t sad_executor_wait(sad_executor_t* ex, uint64_t ticket);
 sad_status_t sad_executor_wait_all(sad_executor_t* ex);
 /* Withdraw a queued request.  *cancelled = 1 when it had not started: it is removed, its

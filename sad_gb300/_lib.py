@@ -62,7 +62,7 @@ class ExecutorConfig(C.Structure):
 
 class RequestResult(C.Structure):
     _fields_ = [("status", i32), ("sites_written", i32), ("psnr", f32), ("queue_ms", C.c_double),
-                ("run_ms", C.c_double), ("message", C.c_char * 192)]
+                ("run_ms", C.c_double), ("message", C.c_char * 192), ("iteration", i32)]
 
 
 # name -> (restype, argtypes)
@@ -155,6 +155,9 @@ SIGNATURES = {
                                      C.POINTER(RequestResult), C.POINTER(C.c_uint64)]),
     "sad_executor_submit_render": (st, [vp, C.POINTER(RenderConfig), vp, u32, i32, i32, vp,
                                         C.POINTER(RequestResult), C.POINTER(C.c_uint64)]),
+    "sad_executor_open_fit": (st, [vp, C.POINTER(TrainConfig), vp, vp, i32, i32, vp, vp, vp]),
+    "sad_executor_submit_continue": (st, [vp, C.c_uint64, i32, vp, i32, vp, vp]),
+    "sad_executor_close_fit": (st, [vp, C.c_uint64, vp, vp]),
     "sad_executor_wait": (st, [vp, C.c_uint64]),
     "sad_executor_wait_all": (st, [vp]),
     "sad_executor_cancel": (st, [vp, C.c_uint64, C.POINTER(i32)]),

@@ -5,7 +5,12 @@
 // host worker threads, each with its own CUDA streams, runs requests concurrently:
 //   * fit: a trainer placed in one stream-ordered slab (sad_trainer_create_in), the whole
 //     schedule, sites and PSNR back to host memory;
-//   * render: sites up, candidate field + render (sad_render_from_sites), pixels back.
+//   * render: sites up, candidate field + render (sad_render_from_sites), pixels back;
+//   * resident fit sessions: open (a trainer placed in its slab, target up, init), any
+//     number of continue requests (more iterations of the same fit -- sites, Adam moments,
+//     candidate fields and device counters stay on the device between requests -- then
+//     sites and PSNR back), close (the slab freed).  A session's slab counts against the
+//     budget from open to close; its requests run one at a time, in submission order.
 // Device memory comes from the device's stream-ordered pool (cudaMallocAsync /
 // cudaFreeAsync): a request's slab is reused by later requests without a device-wide
 // synchronisation (cudaFree would wait for every stream).  Admission is first in, first
@@ -20,6 +25,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <unordered_set>
 #include <vector>
 
@@ -29,9 +35,13 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+enum Kind { kFit = 0, kRender = 1, kOpen = 2, kContinue = 3, kClose = 4 };
+
 struct Request {
     uint64_t ticket = 0;
-    int kind = 0;  // 0 fit, 1 render
+    int kind = 0;  // Kind
+    uint64_t session = 0;  // kOpen / kContinue / kClose
+    int iterations = 0;    // kContinue
     sad_train_config_t tcfg{};
     sad_render_config_t rcfg{};
     const float* target = nullptr;
@@ -62,6 +72,19 @@ void set_message(sad_request_result_t* r, sad_status_t st) {
     }
 }
 
+// A resident fit: its trainer lives in its slab from open to close.
+struct Session {
+    sad_trainer_t* trainer = nullptr;
+    void* mem = nullptr;
+    size_t need = 0;
+    int total_iterations = 0;  // the schedule's length (its configuration's iterations)
+    bool closing = false;  // a close request is queued: no further requests
+    bool opened = false;  // the open request has run (successfully or not)
+    bool failed = false;  // the open request failed: later requests report it
+    bool busy = false;    // one of its requests is running
+    std::string error;
+};
+
 }  // namespace
 
 struct sad_executor {
@@ -75,6 +98,8 @@ struct sad_executor {
     uint64_t next_ticket = 1;
     std::deque<Request> queue;
     std::unordered_set<uint64_t> inflight;  // queued or running
+    uint64_t next_session = 1;
+    std::unordered_map<uint64_t, Session> sessions;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::vector<std::thread> workers;
@@ -113,6 +138,38 @@ sad_status_t run_render(const Request& q, void* mem, cudaStream_t ws) {
     return sad::check_cuda(cudaStreamSynchronize(ws), "executor render: sync");
 }
 
+// Session requests run on the session's trainer, outside the executor's lock (the session
+// is marked busy, so no other worker touches it meanwhile).
+sad_status_t run_open(const Request& q, Session& ss, void* mem, sad_request_result_t* r) {
+    sad::NvtxRange r_nvtx("executor open fit session");
+    sad_trainer_t* t = nullptr;
+    SAD_TRY(sad_trainer_create_in(&q.tcfg, q.w, q.h, mem, q.need, &t));
+    sad_status_t st = sad_trainer_set_target_host(t, q.target, q.mask);
+    if (st == SAD_OK) st = sad_trainer_init(t, nullptr, 0);
+    if (st == SAD_OK) st = sad_trainer_render(t, nullptr, &r->psnr);
+    if (st != SAD_OK) {
+        sad_trainer_destroy(t);
+        return st;
+    }
+    ss.trainer = t;
+    ss.mem = mem;
+    return SAD_OK;
+}
+
+sad_status_t run_continue(const Request& q, Session& ss, sad_request_result_t* r) {
+    sad::NvtxRange r_nvtx("executor continue fit session");
+    sad_trainer_info_t info{};
+    SAD_TRY(sad_trainer_info(ss.trainer, &info));
+    const int end = std::min(ss.total_iterations, info.iteration + std::max(0, q.iterations));
+    SAD_TRY(sad_trainer_run(ss.trainer, end));
+    SAD_TRY(sad_trainer_render(ss.trainer, nullptr, &r->psnr));
+    int written = 0;
+    if (q.capacity > 0) SAD_TRY(sad_trainer_get_sites(ss.trainer, q.sites_out, q.capacity, 1, &written));
+    r->sites_written = written;
+    r->iteration = end;
+    return SAD_OK;
+}
+
 void worker_main(sad_executor* ex) {
     // a worker whose device or stream cannot be set up still takes requests and fails
     // each with that error, so no waiter is left behind
@@ -135,12 +192,30 @@ void worker_main(sad_executor* ex) {
             std::unique_lock<std::mutex> lock(ex->mu);
             // the earliest queued request that fits the memory budget and, for a fit, the
             // cap on running fits (so renders pass fits that wait for a fit slot)
+            // (a session's requests wait while another of its requests runs, and follow
+            // its open request)
+            // Under memory pressure, requests that need memory keep first-in-first-out order
+            // behind the first one that does not fit; requests that need none (a session's
+            // continue and close) may pass it, so a session can always finish and release.
+            std::unordered_set<uint64_t> passed;  // sessions with an earlier queued request
             auto pick = [&]() -> std::deque<Request>::iterator {
+                passed.clear();
+                bool blocked = false;
                 for (auto it = ex->queue.begin(); it != ex->queue.end(); ++it) {
+                    if (it->session) {
+                        // a request of a session that no longer exists runs (and fails) at once
+                        auto ss = ex->sessions.find(it->session);
+                        bool ready = ss == ex->sessions.end() ||
+                                     (!ss->second.busy && (it->kind == kOpen || ss->second.opened) &&
+                                      !passed.count(it->session));
+                        passed.insert(it->session);
+                        if (!ready) continue;
+                    }
+                    if (blocked && it->need > 0) continue;
                     bool mem = ex->budget == 0 || ex->in_use == 0 || ex->in_use + it->need <= ex->budget;
-                    bool slot = it->kind != 0 || ex->max_fits == 0 || ex->running_fits < ex->max_fits;
+                    bool slot = it->kind != kFit || ex->max_fits == 0 || ex->running_fits < ex->max_fits;
                     if (mem && slot) return it;
-                    if (!mem) break;  // keep first-in-first-out order under memory pressure
+                    if (!mem) blocked = true;
                 }
                 return ex->queue.end();
             };
@@ -150,7 +225,11 @@ void worker_main(sad_executor* ex) {
             q = *it;
             ex->queue.erase(it);
             ex->in_use += q.need;
-            if (q.kind == 0) ++ex->running_fits;
+            if (q.kind == kFit) ++ex->running_fits;
+            if (q.session) {
+                auto ss = ex->sessions.find(q.session);
+                if (ss != ex->sessions.end()) ss->second.busy = true;
+            }
             if (ex->inject_slab_failures > 0) {
                 --ex->inject_slab_failures;
                 refused = true;
@@ -167,19 +246,66 @@ void worker_main(sad_executor* ex) {
             sad::set_error("executor: slab allocation refused (injected failure)");
             st = SAD_ERR_OUT_OF_MEMORY;
         }
-        if (st == SAD_OK) st = sad::check_cuda(cudaMallocAsync(&mem, q.need, ws), "executor: slab allocation");
-        if (st == SAD_OK) st = sad::check_cuda(cudaStreamSynchronize(ws), "executor: slab allocation");
-        if (st == SAD_OK) st = q.kind == 0 ? run_fit(q, mem, r) : run_render(q, mem, ws);
+        Session* ss = nullptr;  // node-stable: unordered_map never moves its elements
+        if (q.session) {
+            std::lock_guard<std::mutex> lock(ex->mu);
+            auto it = ex->sessions.find(q.session);
+            if (it != ex->sessions.end()) ss = &it->second;
+        }
+        if (st == SAD_OK && q.session && !ss) {
+            sad::set_error("executor session: closed");
+            st = SAD_ERR_INVALID_ARGUMENT;
+        }
+        if (st == SAD_OK && ss && q.kind == kContinue && ss->failed) {
+            sad::set_error("executor session: %s", ss->error.c_str());
+            st = SAD_ERR_INVALID_ARGUMENT;
+        }
+        if (st == SAD_OK && q.need > 0) {
+            st = sad::check_cuda(cudaMallocAsync(&mem, q.need, ws), "executor: slab allocation");
+            if (st == SAD_OK) st = sad::check_cuda(cudaStreamSynchronize(ws), "executor: slab allocation");
+        }
+        bool keep_slab = false;  // an opened session keeps its slab and its share of the budget
+        size_t release = q.need;
+        if (st == SAD_OK) {
+            switch (q.kind) {
+            case kFit: st = run_fit(q, mem, r); break;
+            case kRender: st = run_render(q, mem, ws); break;
+            case kOpen:
+                st = run_open(q, *ss, mem, r);
+                keep_slab = st == SAD_OK;
+                break;
+            case kContinue: st = run_continue(q, *ss, r); break;
+            case kClose:
+                // the slab (and its share of the budget) is held only after a successful open
+                release = ss->trainer ? ss->need : 0;
+                if (ss->trainer) sad_trainer_destroy(ss->trainer);  // synchronises its streams
+                ss->trainer = nullptr;
+                mem = ss->mem;  // freed below
+                ss->mem = nullptr;
+                break;
+            }
+        }
         set_message(r, st);
-        if (mem) {
+        if (mem && !keep_slab) {
             cudaFreeAsync(mem, ws);
             cudaStreamSynchronize(ws);
         }
         r->run_ms = std::chrono::duration<double, std::milli>(Clock::now() - start).count();
         {
             std::lock_guard<std::mutex> lock(ex->mu);
-            ex->in_use -= q.need;
-            if (q.kind == 0) --ex->running_fits;
+            if (!keep_slab) ex->in_use -= release;
+            if (q.kind == kFit) --ex->running_fits;
+            if (ss) {
+                ss->busy = false;
+                if (q.kind == kOpen) {
+                    ss->opened = true;
+                    if (st != SAD_OK) {
+                        ss->failed = true;
+                        ss->error = r->message;
+                    }
+                }
+                if (q.kind == kClose && st == SAD_OK) ex->sessions.erase(q.session);
+            }
             ex->inflight.erase(q.ticket);
         }
         ex->cv_done.notify_all();
@@ -283,6 +409,82 @@ extern "C" sad_status_t sad_executor_submit_render(sad_executor_t* ex, const sad
     q.result = result;
     q.need = render_need(*cfg, site_count, width, height);
     return enqueue(ex, std::move(q), ticket);
+}
+
+extern "C" sad_status_t sad_executor_open_fit(sad_executor_t* ex, const sad_train_config_t* cfg,
+                                              const float* target_host, const float* mask_host, int width,
+                                              int height, sad_request_result_t* result, uint64_t* session,
+                                              uint64_t* ticket) {
+    sad::clear_error();
+    SAD_REQUIRE(ex && cfg && target_host && result && session, "sad_executor_open_fit: null argument");
+    size_t need = sad_trainer_memory_bytes(cfg, width, height);
+    SAD_REQUIRE(need > 0, "sad_executor_open_fit: invalid configuration or size");
+    std::memset(result, 0, sizeof(*result));
+    Request q;
+    q.kind = kOpen;
+    q.tcfg = *cfg;
+    q.target = target_host;
+    q.mask = mask_host;
+    q.w = width;
+    q.h = height;
+    q.result = result;
+    q.need = need;
+    {
+        std::lock_guard<std::mutex> lock(ex->mu);
+        SAD_REQUIRE(!ex->stop, "sad_executor: destroyed");
+        q.session = ex->next_session++;
+        Session& ss = ex->sessions[q.session];
+        ss.need = need;
+        ss.total_iterations = cfg->iterations;
+    }
+    *session = q.session;
+    return enqueue(ex, std::move(q), ticket);
+}
+
+// Queues a continue or close request of a live session (one whose close is not queued).
+static sad_status_t session_request(sad_executor_t* ex, uint64_t session, Request&& q, uint64_t* ticket,
+                                    const char* who) {
+    {
+        std::lock_guard<std::mutex> lock(ex->mu);
+        auto it = ex->sessions.find(session);
+        if (it == ex->sessions.end() || it->second.closing) {
+            sad::set_error("%s: unknown or closed session", who);
+            return SAD_ERR_INVALID_ARGUMENT;
+        }
+        if (q.kind == kClose) it->second.closing = true;
+    }
+    q.session = session;
+    return enqueue(ex, std::move(q), ticket);
+}
+
+extern "C" sad_status_t sad_executor_submit_continue(sad_executor_t* ex, uint64_t session, int iterations,
+                                                     float* sites_host, int capacity,
+                                                     sad_request_result_t* result, uint64_t* ticket) {
+    sad::clear_error();
+    SAD_REQUIRE(ex && result, "sad_executor_submit_continue: null argument");
+    SAD_REQUIRE(iterations >= 0, "sad_executor_submit_continue: negative iterations");
+    SAD_REQUIRE(capacity == 0 || sites_host, "sad_executor_submit_continue: null sites buffer");
+    std::memset(result, 0, sizeof(*result));
+    Request q;
+    q.kind = kContinue;
+    q.iterations = iterations;
+    q.sites_out = sites_host;
+    q.capacity = capacity;
+    q.result = result;
+    q.need = 0;
+    return session_request(ex, session, std::move(q), ticket, "sad_executor_submit_continue");
+}
+
+extern "C" sad_status_t sad_executor_close_fit(sad_executor_t* ex, uint64_t session, sad_request_result_t* result,
+                                               uint64_t* ticket) {
+    sad::clear_error();
+    SAD_REQUIRE(ex && result, "sad_executor_close_fit: null argument");
+    std::memset(result, 0, sizeof(*result));
+    Request q;
+    q.kind = kClose;
+    q.result = result;
+    q.need = 0;
+    return session_request(ex, session, std::move(q), ticket, "sad_executor_close_fit");
 }
 
 extern "C" sad_status_t sad_executor_wait(sad_executor_t* ex, uint64_t ticket) {

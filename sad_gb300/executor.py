@@ -6,6 +6,9 @@
         sites, psnr = f.result()
         rgb = r.result()
 
+Resident fits: `s = ex.open_fit(image, ...)`, then `s.continue_fit(k)` requests (more
+iterations of the same fit, its state kept on the device), then `s.close()`.
+
 The executor holds every request (and so the host arrays its worker reads and writes)
 until the request completes, whether or not the caller keeps it.  Results are bitwise those
 of a single fit (sad_trainer_fit_host) or render (sad_render_from_sites) of the same input.
@@ -54,7 +57,43 @@ class _Request:
         self.wait()
         if self.kind == "fit":
             return self._out[: self.res.sites_written].copy(), float(self.res.psnr)
+        if self.kind == "continue":
+            return self._out[: self.res.sites_written].copy(), float(self.res.psnr), int(self.res.iteration)
+        if self.kind in ("open", "close"):
+            return float(self.res.psnr)
         return self._out
+
+
+class FitSession:
+    """A resident fit (sad_executor_open_fit): its sites, Adam moments and candidate fields
+    stay on the device between continue() requests, until close()."""
+
+    def __init__(self, ex: "Executor", session: int, opened: _Request, capacity: int):
+        self._ex = ex
+        self.id = session
+        self.opened = opened
+        self._capacity = capacity
+        self.closed = False
+
+    def continue_fit(self, iterations: int, sites: bool = True) -> _Request:
+        """Queue `iterations` more iterations; result() gives (active sites, PSNR, iterations
+        run so far)."""
+        cap = self._capacity if sites else 0
+        out = np.zeros((max(cap, 1), 10), np.float32)
+        req = _Request(self._ex, "continue", (), out)
+        self._ex._check(self._ex._lib.sad_executor_submit_continue(
+            self._ex._h, self.id, int(iterations), out.ctypes.data_as(C.c_void_p), cap, C.byref(req.res),
+            C.byref(req.ticket)))
+        self._ex._pending[req.ticket.value] = req
+        return req
+
+    def close(self) -> _Request:
+        req = _Request(self._ex, "close", (), np.zeros(0, np.float32))
+        self._ex._check(self._ex._lib.sad_executor_close_fit(self._ex._h, self.id, C.byref(req.res),
+                                                             C.byref(req.ticket)))
+        self._ex._pending[req.ticket.value] = req
+        self.closed = True
+        return req
 
 
 class Executor:
@@ -93,6 +132,27 @@ class Executor:
             out.ctypes.data_as(C.c_void_p), cap, C.byref(req.res), C.byref(req.ticket)))
         self._pending[req.ticket.value] = req
         return req
+
+    def open_fit(self, image: np.ndarray, mask: np.ndarray | None = None,
+                 config: _lib.TrainConfig | None = None, **overrides) -> FitSession:
+        """Start a resident fit session (target up, init); see FitSession."""
+        img = np.ascontiguousarray(image, dtype=np.float32)
+        h, w = img.shape[:2]
+        cfg = config if config is not None else _lib.TrainConfig()
+        if config is None:
+            self._lib.sad_train_config_default(C.byref(cfg))
+            cfg.log_freq = 0
+        for k, v in overrides.items():
+            setattr(cfg, k, v)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+        req = _Request(self, "open", (img, m, cfg), np.zeros(0, np.float32))
+        sid = C.c_uint64(0)
+        self._check(self._lib.sad_executor_open_fit(
+            self._h, C.byref(cfg), img.ctypes.data_as(C.c_void_p),
+            None if m is None else m.ctypes.data_as(C.c_void_p), w, h, C.byref(req.res), C.byref(sid),
+            C.byref(req.ticket)))
+        self._pending[req.ticket.value] = req
+        return FitSession(self, sid.value, req, max(cfg.max_sites, cfg.n_sites, 2 * w * h))
 
     def submit_render(self, sites: np.ndarray, width: int, height: int,
                       config: _lib.RenderConfig | None = None) -> _Request:
