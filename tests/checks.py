@@ -44,12 +44,17 @@ def assert_close_sum(got, want, absw, rtol=1e-3, atol=1e-6, what="gradient"):
                              f"worst (index, got, want, abs-sum): {rows}")
 
 
-def assert_grads_close(got, want, absw, rel_l2=1e-3, guard=0.05, atol=1e-6):
+def assert_grads_close(got, want, absw, rel_l2=1e-3, guard=5e-3, atol=1e-6):
     """Per-site parameter gradients ([10, n]): each parameter's gradient vector within a
     relative L2 error of `rel_l2` of the oracle's, and every entry within `guard` of its
-    absolute-contribution sum.  A sum dominated by one pixel whose terms cancel inside
-    candidate_grads (FMA contraction on the GPU, none in the oracle) can be a few percent
-    off on its own; the vector norm and the guard still catch any systematic error."""
+    absolute-contribution sum (plus atol, which also covers the 2^-24 quantum of the
+    fixed-point sums).  The entry bound is relative to the sum of the entry's absolute
+    pixel terms, not to the entry, because the sums are of float terms in different orders
+    (float atomics, FMA contraction on the GPU and none in the oracle) and an entry whose
+    terms cancel has no relative accuracy to hold.  Measured worst case over the GPU test
+    inputs: 1.1e-3 of the sum on a random field (a far candidate's FP32 term is
+    ill-conditioned), at most 1.1e-4 on nearest-site fields; the default 5e-3 leaves a
+    factor of about five."""
     for k in range(got.shape[0]):
         num = np.linalg.norm(got[k] - want[k])
         den = max(np.linalg.norm(want[k]), 1e-12)

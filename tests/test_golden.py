@@ -18,7 +18,7 @@ called through the C ABI, to the same outputs.  Tolerances:
     because the reference sums float terms with atomics in no fixed order and entries
     whose terms cancel have no relative accuracy to hold;
   * per-site gradients: relative L2 error per parameter <= 1e-4 (oracle) / 1e-3 (GPU),
-    every entry within 1% / 5% of its sum of absolute pixel terms (the reference sums
+    every entry within 1% / 0.5% of its sum of absolute pixel terms (the reference sums
     with float atomics in no fixed order);
   * removal delta 1e-3 relative; tau diffusion and Adam 2e-6; site statistics 2e-4
     relative; densify keys within 2 ulps of the reference's powf; split positions 1e-4

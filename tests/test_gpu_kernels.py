@@ -9,9 +9,10 @@ Tolerances (stated here, used below):
   * candidate lists from distance ranking: identical except where two distances agree to
     1e-5 relative (CPU libm expf / no-FMA vs CUDA), and identical lists on >= 99% pixels;
   * rendered RGB: max abs error <= 1e-4;
-  * per-site gradients: relative L2 error per parameter <= 1e-3 and every entry within 5%
-    of its sum of absolute pixel terms (the oracle sums in double without FMA; the API
-    kernels sum with float atomics in no fixed order, like the reference).
+  * per-site gradients: relative L2 error per parameter <= 1e-3 and every entry within
+    0.5% of its sum of absolute pixel terms (the oracle sums in double without FMA; the API
+    kernels sum with float atomics in no fixed order, like the reference; measured worst
+    case 0.11%, checks.assert_grads_close).
 """
 import numpy as np
 import pytest
