@@ -212,6 +212,18 @@ def compute_gradients(c0, c1, target, sites, w, h, mask=None, rendered=None, ssi
     return g, a, rem
 
 
+def compute_gradients_d(c0, c1, target, sites, w, h, mask=None):
+    """FP64 form of compute_gradients' ten per-site sums for the MSE loss (no SSIM term):
+    the render adjoint of dL/dpred = 2 (pred - target) on the pixels the mask keeps, with
+    pred and every term in double.  Returns [10, N] float64."""
+    inv_s2 = 1.0 / float(max(w, h)) ** 2
+    s64 = np.asarray(sites, np.float64)
+    gout = 2.0 * (render_d(c0, c1, s64, w, h, inv_s2) - np.asarray(target, np.float64))
+    if mask is not None:
+        gout *= (np.asarray(mask) > 0)[..., None]
+    return render_backward_d(c0, c1, s64, gout, w, h, inv_s2).T
+
+
 def tau_diffuse(c0, c1, sites, raw, gin, lam, w, h, ds=1):
     c0, c1, sites = _c(c0, np.uint32), _c(c1, np.uint32), _c(sites, np.float32)
     raw, gin = _c(raw, np.float32), _c(gin, np.float32)

@@ -33,9 +33,10 @@ def raw_dist_np(sites, ids, xs, ys, inv_s2):
     return np.where(ok, d, np.inf)
 
 
-def assert_close_sum(got, want, absw, rtol=1e-3, atol=1e-6, what="gradient"):
-    """|got - want| <= rtol * absw + atol elementwise, reporting the worst violations."""
-    err = np.abs(got - want) - (rtol * absw + atol)
+def assert_close_sum(got, want, absw, rtol=1e-3, atol=1e-6, what="gradient", band=0.0):
+    """|got - want| <= rtol * absw + atol + band elementwise, reporting the worst
+    violations."""
+    err = np.abs(got - want) - (rtol * absw + atol + band)
     if np.any(err > 0):
         idx = np.argsort(err.ravel())[::-1][:8]
         rows = [(np.unravel_index(i, err.shape), float(got.ravel()[i]), float(want.ravel()[i]),
@@ -44,7 +45,7 @@ def assert_close_sum(got, want, absw, rtol=1e-3, atol=1e-6, what="gradient"):
                              f"worst (index, got, want, abs-sum): {rows}")
 
 
-def assert_grads_close(got, want, absw, rel_l2=1e-3, guard=5e-3, atol=1e-6):
+def assert_grads_close(got, want, absw, rel_l2=1e-3, guard=5e-3, atol=1e-6, want64=None):
     """Per-site parameter gradients ([10, n]): each parameter's gradient vector within a
     relative L2 error of `rel_l2` of the oracle's, and every entry within `guard` of its
     absolute-contribution sum (plus atol, which also covers the 2^-24 quantum of the
@@ -52,14 +53,23 @@ def assert_grads_close(got, want, absw, rel_l2=1e-3, guard=5e-3, atol=1e-6):
     pixel terms, not to the entry, because the sums are of float terms in different orders
     (float atomics, FMA contraction on the GPU and none in the oracle) and an entry whose
     terms cancel has no relative accuracy to hold.  Measured worst case over the GPU test
-    inputs: 1.1e-3 of the sum on a random field (a far candidate's FP32 term is
-    ill-conditioned), at most 1.1e-4 on nearest-site fields; the default 5e-3 leaves a
-    factor of about five."""
+    inputs on nearest-site fields (what a fit sees): 1.1e-4 of the sum; the default 5e-3
+    leaves a factor of forty.
+
+    want64, the oracle's FP64 form of the same sums, widens each entry's bound by twice
+    |want - want64|: where the FP32 result itself is ill-conditioned an FP32 kernel may
+    land anywhere that close to the exact value.  Random candidate fields are such inputs:
+    a far candidate's term depends on perp2 = |d|^2 - proj^2, which cancels, so the FP32
+    and FP64 oracles differ there by up to 3.7% (loss gradients, 128x128 with 2000 sites)
+    and 11% (render adjoint, 200x130 with 3000 sites) of an entry's absolute sum, and the
+    GPU kernels land closer to the FP64 value than the FP32 oracle does."""
     for k in range(got.shape[0]):
         num = np.linalg.norm(got[k] - want[k])
         den = max(np.linalg.norm(want[k]), 1e-12)
-        assert num <= rel_l2 * den + atol * np.sqrt(got.shape[1]), (k, num / den)
-    assert_close_sum(got, want, absw, rtol=guard, atol=atol)
+        band = 0.0 if want64 is None else 2.0 * np.linalg.norm(want[k] - want64[k])
+        assert num <= rel_l2 * den + band + atol * np.sqrt(got.shape[1]), (k, num / den)
+    band = 0.0 if want64 is None else 2.0 * np.abs(want - want64)
+    assert_close_sum(got, want, absw, rtol=guard, atol=atol, band=band)
 
 
 def assert_lists_match(got, want, dist_fn, w, h, min_exact=0.99):

@@ -12,7 +12,10 @@ Tolerances (stated here, used below):
   * per-site gradients: relative L2 error per parameter <= 1e-3 and every entry within
     0.5% of its sum of absolute pixel terms (the oracle sums in double without FMA; the API
     kernels sum with float atomics in no fixed order, like the reference; measured worst
-    case 0.11%, checks.assert_grads_close).
+    case 0.11% on nearest-site fields, checks.assert_grads_close); on random fields, where
+    a far candidate's FP32 term is itself ill-conditioned, an entry may also differ by
+    twice the gap between the FP32 and FP64 oracles (MSE loss gradients and the render
+    adjoint, which have FP64 forms).
 """
 import numpy as np
 import pytest
@@ -95,8 +98,10 @@ def test_render_backward_matches_oracle(ops, orc, w, h, n, seed, field, log_tau)
     gout = np.random.default_rng(seed).normal(size=(h, w, 3)).astype(np.float32)
     got = ops.render_sad_backward(t32(c0), t32(c1), tf(sites), tf(gout), 1.0 / max(w, h) ** 2, w, h)
     want, absw = orc.render_backward(c0, c1, sites, gout, w, h)
+    want64 = orc.render_backward_d(c0, c1, sites.astype(np.float64), gout.astype(np.float64), w, h,
+                                   1.0 / max(w, h) ** 2)
     got = got.cpu().numpy().astype(np.float64)
-    assert_grads_close(got.T, want.T, absw.T)
+    assert_grads_close(got.T, want.T, absw.T, want64=want64.T)
 
 
 def test_autograd_function_and_fp64_finite_differences(cuda, orc):
@@ -240,8 +245,9 @@ def test_fused_gradients_match_oracle(ops, orc, w, h, n, removal, masked, ssim):
                                 1.0 / max(w, h) ** 2, 0, int(removal), ssim, w, h)
     g, a, rem = orc.compute_gradients(c0, c1, img, sites, w, h, mask=mask if masked else None,
                                       rendered=rendered, ssim_weight=ssim, removal=removal)
+    want64 = orc.compute_gradients_d(c0, c1, img, sites, w, h, mask if masked else None) if ssim == 0 else None
     got = np.stack([b.cpu().numpy() for b in bufs[:10]]).astype(np.float64)
-    assert_grads_close(got, g, a)
+    assert_grads_close(got, g, a, want64=want64)
     if removal:
         r = bufs[10].cpu().numpy().astype(np.float64)
         assert np.all(np.abs(r - rem) <= 1e-3 * np.maximum(np.abs(rem), 1.0) + 1e-4)
@@ -297,7 +303,8 @@ def test_trainer_gradients_match_oracle(ops, orc, w, h, n, field, removal, maske
     got = fix[:, :10].T.astype(np.float64) / 2.0 ** 24
     g, a, rem = orc.compute_gradients(c0, c1, img, sites, w, h, mask=mask if masked else None,
                                       rendered=rendered, ssim_weight=ssim, removal=removal)
-    assert_grads_close(got, g, a)
+    want64 = orc.compute_gradients_d(c0, c1, img, sites, w, h, mask if masked else None) if ssim == 0 else None
+    assert_grads_close(got, g, a, want64=want64)
     bufs = _grad_buffers(n)
     ops.compute_gradients_tiled(t32(c0), t32(c1), tf(img), tf(rendered), tf(mask), tf(sites), *bufs,
                                 1.0 / max(w, h) ** 2, 0, int(removal), ssim, w, h)
