@@ -203,48 +203,67 @@ struct TileValues<NV, N, AccSplit> {
     }
 };
 
-// Fixed-point values with the lo words privatised per lane group: lanes of different
-// groups that reach the same entry at the same instruction hit different words, and the
-// copies are offset by 16 words so those words sit in different banks.  Adds follow
-// TileValues<.., AccSplit>::add_unique (at most one add per pixel and entry); the hi words
-// (rare) are shared.
-template <int NV, int N, int COPIES>
-struct PrivatisedValues {
-    static constexpr int kStride = NV * N + 16;
-    int lo[COPIES * kStride];
-    int hi[NV][N];
+// Fixed-point lo words of a precomputed tile table, privatised per lane group so that lanes
+// adding to the same entry at the same instruction mostly hit different words (such
+// same-address lanes serialise; with an 8-site nearest list per pixel, a warp's 32 lanes
+// reach only 10-20 distinct sites per step).  The words form four banks-apart blocks of
+// kNarrowKeys entries, used in one of two ways chosen per tile from its key count:
+//   narrow (at most kNarrowKeys entries): block = the pixel's row in its 8x4 warp patch, so
+//     each entry has four copies;
+//   wide (up to kTileKeys entries): block = 2 * (entry / kNarrowKeys) + row parity, so each
+//     entry has two copies.
+// Both address a word as block * kStride + value * kNarrowKeys + entry % kNarrowKeys, so
+// one accumulation loop serves both.  Adds follow TileValues<.., AccSplit>::add_unique (at
+// most one add per pixel and entry: a copy sums at most 128 single-word terms of |x| <=
+// 2^22); the hi words (rare) are shared.
+constexpr int kNarrowKeys = kTileKeys / 2;
 
-    __device__ __forceinline__ void zero(int d) {
+template <int NV>
+struct TileWords {
+    static constexpr int kStride = NV * kNarrowKeys + 8;  // blocks 8 banks apart
+    int lo[4 * kStride];
+    int hi[NV][kTileKeys];
+
+    // the row bits of a lane in pixel row `row` (0-3) of its warp patch, and the block of
+    // entry d for those bits (a narrow tile's entries are all below kNarrowKeys)
+    static __device__ __forceinline__ int row_bits(int row, bool wide) { return row & (wide ? 1 : 3); }
+    static __device__ __forceinline__ int block_of(int d, int rbits) { return ((d / kNarrowKeys) << 1) | rbits; }
+    __device__ __forceinline__ int* word(int block, int d) { return lo + block * kStride + d % kNarrowKeys; }
+    __device__ __forceinline__ const int* word(int block, int d) const {
+        return lo + block * kStride + d % kNarrowKeys;
+    }
+
+    __device__ __forceinline__ void zero(int d, bool wide) {
+        const int b0 = wide ? (d / kNarrowKeys) << 1 : 0, nb = wide ? 2 : 4;
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             hi[k][d] = 0;
-#pragma unroll
-            for (int c = 0; c < COPIES; ++c) lo[c * kStride + k * N + d] = 0;
+            for (int b = b0; b < b0 + nb; ++b) word(b, d)[k * kNarrowKeys] = 0;
         }
     }
-    __device__ __forceinline__ void add_unique(int d, const float (&v)[NV], int copy) {
-        int* lc = lo + copy * kStride + d;
+    __device__ __forceinline__ void add_unique(int d, int block, const float (&v)[NV]) {
+        int* lc = word(block, d);
         float m = 0.0f;
 #pragma unroll
         for (int k = 0; k < NV; ++k) m = fmaxf(m, fabsf(v[k]));
         if (m < 0.25f) {
 #pragma unroll
             for (int k = 0; k < NV; ++k)
-                atomicAdd(lc + k * N, __float_as_int(fmaf(v[k], kFixScale, 12582912.0f)) - 0x4B400000);
+                atomicAdd(lc + k * kNarrowKeys, __float_as_int(fmaf(v[k], kFixScale, 12582912.0f)) - 0x4B400000);
         } else {
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
                 int h, l;
                 split_fix(v[k], h, l);
-                atomicAdd(lc + k * N, l);
+                atomicAdd(lc + k * kNarrowKeys, l);
                 if (h != 0) atomicAdd(&hi[k][d], h);
             }
         }
     }
-    __device__ __forceinline__ long long fixed(int k, int d) const {
+    __device__ __forceinline__ long long fixed(int k, int d, bool wide) const {
+        const int b0 = wide ? (d / kNarrowKeys) << 1 : 0, nb = wide ? 2 : 4;
         long long x = static_cast<long long>(hi[k][d]) * (1ll << kSplitLoBits);
-#pragma unroll
-        for (int c = 0; c < COPIES; ++c) x += static_cast<long long>(lo[c * kStride + k * N + d]);
+        for (int b = b0; b < b0 + nb; ++b) x += static_cast<long long>(word(b, d)[k * kNarrowKeys]);
         return x;
     }
 };
@@ -313,12 +332,15 @@ __device__ __forceinline__ uint32_t lane_rotation() {
 }
 
 // Registration of one pixel's candidate list into its tile's table (all 32 lanes of the
-// warp call it); writes the packed 8 x u16 table indices (0xFFFF: none) to the slot map.
+// warp call it); writes the packed 8 x u16 table indices (0xFFFF: none) to the slot map and
+// returns how many of them name an entry at or past kNarrowKeys (a far entry: keys are
+// claimed nearest candidate first, so those are the tile's far, low-weight candidates).
 template <class Table, class Map>
-__device__ __forceinline__ void register_tile_pixel(Table& table, const uint32_t (&ids)[8],
-                                                    uint32_t n, int x, int y, int w, bool inside,
-                                                    const Map& map) {
+__device__ __forceinline__ int register_tile_pixel(Table& table, const uint32_t (&ids)[8],
+                                                   uint32_t n, int x, int y, int w, bool inside,
+                                                   const Map& map) {
     uint32_t packed[4] = {0u, 0u, 0u, 0u};
+    int far = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         int slot = register_key(table, ids[i] < n ? ids[i] : kEmpty);
@@ -328,19 +350,31 @@ __device__ __forceinline__ void register_tile_pixel(Table& table, const uint32_t
 #pragma unroll
         for (int j = 0; j < i; ++j) repeat |= ids[j] == ids[i];
         uint32_t sidx = (slot < 0 || slot >= kTileKeys || repeat) ? 0xFFFFu : static_cast<uint32_t>(slot);
+        far += (sidx != 0xFFFFu && sidx >= static_cast<uint32_t>(kNarrowKeys)) ? 1 : 0;
         packed[i >> 1] |= sidx << (16 * (i & 1));
     }
     if (inside)
         map.slot_map[static_cast<size_t>(y) * w + x] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    return inside ? far : 0;
 }
 
-// After the tile's registrations (and a barrier): its key list and count.
+// A tile's word-table shape (TileWords): wide when more than this many of its (pixel,
+// candidate) references name far entries, narrow (far entries take the global path)
+// otherwise.  Narrow gives the hot entries four copies instead of two; a tile whose far
+// entries carry an eighth of its 2048 references is cheaper to keep whole in the table.
+constexpr int kWideFarRefs = 256;
+// tile_count word: keys in use, plus this flag for a wide tile
+constexpr int kTileWideFlag = 1 << 30;
+
+// After the tile's registrations (and a barrier): its key list, and its key count with the
+// shape flag (far_refs: the tile's summed register_tile_pixel results).
 template <class Table, class Map>
-__device__ __forceinline__ void write_tile_keys(const Table& table, int tid, int tile, const Map& map) {
+__device__ __forceinline__ void write_tile_keys(const Table& table, int tid, int tile, int far_refs,
+                                                const Map& map) {
     const int used = min(table.size(), kTileKeys);
     for (int d = tid; d < used; d += 256)
         map.tile_keys[static_cast<size_t>(tile) * kTileKeys + d] = table.key_at(d);
-    if (tid == 0) map.tile_count[tile] = used;
+    if (tid == 0) map.tile_count[tile] = used | (far_refs > kWideFarRefs ? kTileWideFlag : 0);
 }
 
 #ifdef __CUDACC__

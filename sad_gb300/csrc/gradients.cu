@@ -108,18 +108,6 @@ __device__ __forceinline__ void flush_slot(const GradParams& p, const Table& tab
     }
 }
 
-// Flush of one table entry of the precomputed-registration kernel (fixed point).
-template <int NV, class Values>
-__device__ __forceinline__ void flush_values(const GradParams& p, const Values& vals, uint32_t key,
-                                             int d) {
-    long long* o = p.fix12 + static_cast<size_t>(key) * 12;
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        long long v = vals.fixed(k, d);
-        if (v != 0) fix_add_global(o + k, v);
-    }
-}
-
 // Values per table slot: 10 gradients, + removal delta (float path), + removal delta and
 // count of "keep < 1e-4" pixels (fixed-point path; each such pixel adds the reference's
 // 1e6 sentinel, kept as an exact integer count so the fixed-point sum cannot overflow).
@@ -131,11 +119,13 @@ struct GradLayout {
     // precomputed registration (trainer): the tile's values, keys and staged sites, and
     // each thread's candidate weights (and removal deltas) for the accumulation loop
     struct Pre {
-        PrivatisedValues<NV, kTileKeys, 2> vals;  // lo words per pixel-row parity
+        TileWords<NV> vals;  // lo words per pixel row (narrow tiles) or row parity (wide)
         uint32_t dkey[kTileKeys];
-        float4 g0[kTileKeys];  // px, py, tau, radius
-        float4 g1[kTileKeys];  // dx, dy, l1, l2
-        float4 col[kTileKeys];  // r, g, b, -
+        // staged site records of the first kNarrowKeys entries (the entries of a wide tile
+        // beyond them read their site from global memory)
+        float4 g0[kNarrowKeys];  // px, py, tau, radius
+        float4 g1[kNarrowKeys];  // dx, dy, l1, l2
+        float4 col[kNarrowKeys];  // r, g, b, -
         float wts[kCand][256];
         float rem[kRemoval ? kCand : 1][256];
     };
@@ -392,19 +382,24 @@ __device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& 
     auto& sm = shared_table<typename L::Pre>();
     const int tid = threadIdx.x;
     const int tile = by * tiles_x + bx;
-    const int used = prm.tile_count[tile];
+    const int tile_word = prm.tile_count[tile];
+    const bool wide = (tile_word & kTileWideFlag) != 0;  // uniform over the block
+    // a narrow tile keeps its first kNarrowKeys entries; slot_of() sends the rest global
+    const int used = wide ? tile_word & ~kTileWideFlag : min(tile_word, kNarrowKeys);
     {
         const uint32_t* keys = prm.tile_keys + static_cast<size_t>(tile) * kTileKeys;
         for (int d = tid; d < used; d += 256) {
             const uint32_t key = keys[d];
             sm.dkey[d] = key;
-            sm.vals.zero(d);
-            SiteGeom g;
-            float3 c;
-            src.load(key, g, c);
-            sm.g0[d] = make_float4(g.px, g.py, g.tau, g.radius);
-            sm.g1[d] = make_float4(g.dx, g.dy, g.l1, g.l2);
-            sm.col[d] = make_float4(c.x, c.y, c.z, 0.0f);
+            sm.vals.zero(d, wide);
+            if (d < kNarrowKeys) {
+                SiteGeom g;
+                float3 c;
+                src.load(key, g, c);
+                sm.g0[d] = make_float4(g.px, g.py, g.tau, g.radius);
+                sm.g1[d] = make_float4(g.dx, g.dy, g.l1, g.l2);
+                sm.col[d] = make_float4(c.x, c.y, c.z, 0.0f);
+            }
         }
     }
     __syncthreads();
@@ -419,19 +414,19 @@ __device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& 
 
     // table index of each candidate, 8 x u16 packed in 4 words (0xFFFF: not in the table)
     uint32_t pm[4] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
-    auto slot_of = [&pm](int i) {
+    auto slot_of = [&pm, used](int i) {
         uint32_t word = (i >> 1) == 0 ? pm[0] : (i >> 1) == 1 ? pm[1] : (i >> 1) == 2 ? pm[2] : pm[3];
         uint32_t sidx = (word >> ((i & 1) << 4)) & 0xFFFFu;
-        return sidx == 0xFFFFu ? -1 : static_cast<int>(sidx);
+        return sidx >= static_cast<uint32_t>(used) ? -1 : static_cast<int>(sidx);
     };
     auto site_at = [&](uint32_t id, int slot, SiteGeom& g, float3& c) {
-        if (slot >= 0) {
+        if (static_cast<unsigned>(slot) < static_cast<unsigned>(kNarrowKeys)) {
             float4 a = sm.g0[slot], b = sm.g1[slot], q = sm.col[slot];
             g.px = a.x; g.py = a.y; g.tau = a.z; g.radius = a.w;
             g.dx = b.x; g.dy = b.y; g.l1 = b.z; g.l2 = b.w;
             c = make_float3(q.x, q.y, q.z);
         } else {
-            src.load(id, g, c);  // not in the tile's table: read directly
+            src.load(id, g, c);  // not staged: read directly
         }
     };
 
@@ -470,6 +465,7 @@ __device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& 
 
     // accumulate in a lane-rotated candidate order
     const uint32_t r = lane_rotation();
+    const int rbits = TileWords<NV>::row_bits(lane >> 3, wide);
 #pragma unroll 1
     for (int j = 0; j < kCand; ++j) {
         const int c = static_cast<int>((j + r) & 7u);
@@ -483,19 +479,29 @@ __device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& 
         if (wt == 0.0f && rv == 0.0f) continue;
         const int slot = slot_of(c);
         uint32_t id = kEmpty;
-        if (slot < 0) id = (c < 4 ? prm.cand0 : prm.cand1)[4 * static_cast<size_t>(ci) + (c & 3)];
+        if (slot < 0)
+            id = (c < 4 ? prm.cand0 : prm.cand1)[4 * static_cast<size_t>(ci) + (c & 3)];
+        else if (slot >= kNarrowKeys)
+            id = sm.dkey[slot];  // a wide tile's entry without a staged site
         SiteGeom g;
         float3 col;
         site_at(id, slot, g, col);
         float v[NV];
         candidate_values<true, NV>(g, col, ux, uy, inv_s2, inv_scale, wt, dLdp, pred, rv, prm.removal_fix_mul, v);
         if (slot >= 0)
-            sm.vals.add_unique(slot, v, (lane >> 3) & 1);
+            sm.vals.add_unique(slot, TileWords<NV>::block_of(slot, rbits), v);
         else
             global_add<true, NV>(prm, id, v);
     }
     __syncthreads();
-    for (int d = tid; d < used; d += 256) flush_values<NV>(prm, sm.vals, sm.dkey[d], d);
+    for (int d = tid; d < used; d += 256) {
+        long long* o = prm.fix12 + static_cast<size_t>(sm.dkey[d]) * 12;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const long long x = sm.vals.fixed(k, d, wide);
+            if (x != 0) fix_add_global(o + k, x);
+        }
+    }
 }
 
 // Tile registration of a candidate field: the table index of each (pixel, candidate)
@@ -535,8 +541,10 @@ __device__ __forceinline__ void register_tile(const uint4* __restrict__ c0, cons
                                               uint32_t n, int w, int h, int cw, int ch, const TileMap& map,
                                               int bx, int by, int tiles_x) {
     __shared__ KeyTable<512> table;
+    __shared__ int s_far;  // the tile's references to far entries
     const int tid = threadIdx.x;
     table.init_keys(tid, 256);
+    if (tid == 0) s_far = 0;
     __syncthreads();
     const int lane = tid & 31, warp = tid >> 5;
     const int x = bx * 16 + (warp & 1) * 8 + (lane & 7);
@@ -552,9 +560,10 @@ __device__ __forceinline__ void register_tile(const uint4* __restrict__ c0, cons
 #pragma unroll
         for (int i = 0; i < kCand; ++i) ids[i] = kEmpty;
     }
-    register_tile_pixel(table, ids, n, x, y, w, inside, map);
+    const int far = __reduce_add_sync(0xffffffffu, register_tile_pixel(table, ids, n, x, y, w, inside, map));
+    if (lane == 0 && far != 0) atomicAdd(&s_far, far);
     __syncthreads();
-    write_tile_keys(table, tid, by * tiles_x + bx, map);
+    write_tile_keys(table, tid, by * tiles_x + bx, s_far, map);
 }
 
 size_t tile_map_words(int w, int h) {

@@ -109,7 +109,7 @@ struct GradParams {
     // (nullptr: register keys inside the gradient kernel)
     const uint4* slot_map;     // [H*W] 8 x u16 tile-table index per candidate, 0xFFFF none
     const uint32_t* tile_keys;  // [tiles][kTileKeys] keys by table index
-    const int* tile_count;      // [tiles] keys in use
+    const int* tile_count;      // [tiles] keys in use | kTileWideFlag for a wide word table
 };
 struct TileMap {
     uint4* slot_map;

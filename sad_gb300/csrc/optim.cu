@@ -124,6 +124,17 @@ __device__ __forceinline__ void tau_first_one(const uint4* __restrict__ c0, cons
     int p = py * w + px;
     uint4 a = __ldg(c0 + p), b = __ldg(c1 + p);
     uint32_t ids[kCand] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    // every candidate's position and raw gradient are fetched before any is used, so the
+    // 16 gathers overlap instead of forming a chain of dependent loads
+    float cpx[kCand];
+    long long cfix[kCand];
+#pragma unroll
+    for (int k = 0; k < kCand; ++k) {
+        const uint32_t m = ids[k];
+        const bool ok = m < n && m != i;
+        cpx[k] = ok ? __ldg(&geom[m].px) : -1.0f;
+        cfix[k] = ok ? fix12[static_cast<size_t>(m) * 12 + 2] : 0ll;
+    }
     uint32_t list[kCand];
     float sum = 0.0f;
     uint32_t cnt = 0;
@@ -131,12 +142,11 @@ __device__ __forceinline__ void tau_first_one(const uint4* __restrict__ c0, cons
     for (int k = 0; k < kCand; ++k) {
         list[k] = kEmpty;
         uint32_t m = ids[k];
-        bool take = m < n && m != i;
+        bool take = cpx[k] >= 0.0f;
 #pragma unroll
         for (int j = 0; j < k; ++j) take &= ids[j] != m;
-        if (take) take = __ldg(&geom[m].px) >= 0.0f;
         if (take) {
-            sum += from_fix(fix12[static_cast<size_t>(m) * 12 + 2]);
+            sum += from_fix(cfix[k]);
             list[k] = m;
             cnt += 1;
         }
@@ -158,12 +168,15 @@ __device__ __forceinline__ float tau_list_pass(const TauLists& tl, const float* 
     if (!(lambda > 0.0f)) return gin[i];
     uint4 a = tl.nbr[2 * i], b = tl.nbr[2 * i + 1];
     uint32_t ids[kCand] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    float v[kCand];
+#pragma unroll
+    for (int k = 0; k < kCand; ++k) v[k] = ids[k] == kEmpty ? 0.0f : gin[ids[k]];  // gathers overlap
     float sum = 0.0f;
     uint32_t cnt = 0;
 #pragma unroll
     for (int k = 0; k < kCand; ++k) {
         if (ids[k] == kEmpty) continue;
-        sum += gin[ids[k]];
+        sum += v[k];
         cnt += 1;
     }
     return (r + lambda * sum) / (1.0f + lambda * static_cast<float>(cnt));
