@@ -374,6 +374,11 @@ typedef struct {
     int use_graphs;                /* replay each iteration kind from a CUDA graph */
     int init_per_pixel;            /* --init-per-pixel: sites given one per pixel, candidates
                                       initialised per pixel (launchInitCandidates' flag) */
+    int autotune;                  /* 1: pick the gradient kernel's tile-table shape rule by
+                                      timing refresh windows during the fit; every rule gives
+                                      the same sums, so the fit is unchanged.  0 (default):
+                                      the fixed rule, which measured as fast or faster at
+                                      256^2-1024^2.  No reference knob. */
 } sad_train_config_t;
 
 /* Fill with the reference's training_config.json values. */
@@ -429,6 +434,10 @@ typedef struct {
     double gpu_ms_gradients; /* summed device time of the fused gradient kernel */
     int gradient_launches;
     uint64_t kernel_launches;
+    int wide_far_refs;      /* tile-table shape rule in use: a tile is wide when more than
+                               this many of its (pixel, candidate) references name far
+                               entries (the autotuner's pick, or the fixed default) */
+    int tune_rounds;        /* autotuner rounds completed in this fit */
 } sad_trainer_info_t;
 sad_status_t sad_trainer_info(sad_trainer_t* t, sad_trainer_info_t* info);
 /* Time the fused gradient kernel with CUDA events on the trainer's stream. */

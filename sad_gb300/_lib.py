@@ -38,7 +38,7 @@ class TrainConfig(C.Structure):
         ("lr_aniso", f32), ("lr_scale", f32), ("init_log_tau", f32), ("init_radius", f32),
         ("init_gradient_alpha", f32), ("beta1", f32), ("beta2", f32), ("eps", f32),
         ("ssim_weight", f32), ("log_freq", i32), ("use_graphs", i32),
-        ("init_per_pixel", i32),
+        ("init_per_pixel", i32), ("autotune", i32),
     ]
 
 
@@ -46,7 +46,8 @@ class TrainerInfo(C.Structure):
     _fields_ = [("width", i32), ("height", i32), ("iteration", i32), ("site_buffer", i32),
                 ("active_estimate", i32), ("capacity", i32), ("prune_percentile", f32),
                 ("densify_percentile", f32), ("gpu_ms_gradients", C.c_double),
-                ("gradient_launches", i32), ("kernel_launches", C.c_uint64)]
+                ("gradient_launches", i32), ("kernel_launches", C.c_uint64),
+                ("wide_far_refs", i32), ("tune_rounds", i32)]
 
 
 class RenderConfig(C.Structure):

@@ -358,10 +358,12 @@ __device__ __forceinline__ int register_tile_pixel(Table& table, const uint32_t 
     return inside ? far : 0;
 }
 
-// A tile's word-table shape (TileWords): wide when more than this many of its (pixel,
+// A tile's word-table shape (TileWords): wide when more than `rule` of its (pixel,
 // candidate) references name far entries, narrow (far entries take the global path)
-// otherwise.  Narrow gives the hot entries four copies instead of two; a tile whose far
-// entries carry an eighth of its 2048 references is cheaper to keep whole in the table.
+// otherwise.  Narrow gives the hot entries four copies instead of two, wide keeps the far
+// entries in shared memory; which costs less depends on the image and the phase of the
+// fit, so the trainer tunes the rule while it runs (every rule gives the same sums).  The
+// default: wide when the far entries carry more than an eighth of the 2048 references.
 constexpr int kWideFarRefs = 256;
 // tile_count word: keys in use, plus this flag for a wide tile
 constexpr int kTileWideFlag = 1 << 30;
@@ -370,11 +372,11 @@ constexpr int kTileWideFlag = 1 << 30;
 // shape flag (far_refs: the tile's summed register_tile_pixel results).
 template <class Table, class Map>
 __device__ __forceinline__ void write_tile_keys(const Table& table, int tid, int tile, int far_refs,
-                                                const Map& map) {
+                                                int rule, const Map& map) {
     const int used = min(table.size(), kTileKeys);
     for (int d = tid; d < used; d += 256)
         map.tile_keys[static_cast<size_t>(tile) * kTileKeys + d] = table.key_at(d);
-    if (tid == 0) map.tile_count[tile] = used | (far_refs > kWideFarRefs ? kTileWideFlag : 0);
+    if (tid == 0) map.tile_count[tile] = used | (far_refs > rule ? kTileWideFlag : 0);
 }
 
 #ifdef __CUDACC__

@@ -54,7 +54,8 @@ struct DevState {
     float adam_c1;      // Adam bias corrections 1 / (1 - beta^t) for t = iter + 1
     float adam_c2;
     uint32_t n_alive;   // length of the compacted active-site list
-    uint32_t pad[3];
+    int32_t wide_far_refs;  // tile-table shape rule of the tile registration (tuned on the host)
+    uint32_t pad[2];
 };
 
 // Programmatic dependent launch: a kernel launched with the programmatic-serialization

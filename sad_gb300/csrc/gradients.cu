@@ -563,7 +563,8 @@ __device__ __forceinline__ void register_tile(const uint4* __restrict__ c0, cons
     const int far = __reduce_add_sync(0xffffffffu, register_tile_pixel(table, ids, n, x, y, w, inside, map));
     if (lane == 0 && far != 0) atomicAdd(&s_far, far);
     __syncthreads();
-    write_tile_keys(table, tid, by * tiles_x + bx, s_far, map);
+    const int rule = map.wide_far_refs ? *map.wide_far_refs : kWideFarRefs;
+    write_tile_keys(table, tid, by * tiles_x + bx, s_far, rule, map);
 }
 
 size_t tile_map_words(int w, int h) {
@@ -577,6 +578,7 @@ TileMap tile_map_at(uint32_t* base, int w, int h) {
     m.slot_map = reinterpret_cast<uint4*>(base);
     m.tile_keys = base + static_cast<size_t>(w) * h * 4;
     m.tile_count = reinterpret_cast<int*>(m.tile_keys + tiles * kTileKeys);
+    m.wide_far_refs = nullptr;
     return m;
 }
 

@@ -115,6 +115,7 @@ struct TileMap {
     uint4* slot_map;
     uint32_t* tile_keys;
     int* tile_count;
+    const int* wide_far_refs;  // device word with the tile-table shape rule (nullptr: kWideFarRefs)
 };
 // Batched launches: one grid over the tiles of every image of a batch; tile_prefix[i] is
 // image i's first block (tile_prefix[n_items] = total_tiles); items and prefixes live in
@@ -223,6 +224,8 @@ void launch_compact_batch(const SiteBatchItem* items, uint32_t n_items, uint32_t
 void launch_clear_f32(float* buf, size_t count, cudaStream_t st);
 // iteration counter, VPT pass counter and the next iteration's Adam bias corrections
 void launch_reset_state(DevState* state, float beta1, float beta2, cudaStream_t st);
+// Set the tile-table shape rule read by the next tile registrations.
+void launch_set_wide_far_refs(DevState* state, int value, cudaStream_t st);
 void launch_advance_state(DevState* state, uint32_t vpt_passes, float beta1, float beta2,
                           cudaStream_t st);
 

@@ -191,6 +191,7 @@ extern "C" void sad_train_config_default(sad_train_config_t* c) {
     c->log_freq = 1000;
     c->use_graphs = 1;
     c->init_per_pixel = 0;
+    c->autotune = 0;
 }
 
 // RenderOptions defaults, backends/cuda/src/sad_cuda.cu:618-637 / 656-670

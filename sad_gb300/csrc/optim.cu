@@ -457,6 +457,7 @@ __device__ __forceinline__ void set_bias_corrections(DevState* state, float beta
 __global__ void reset_state_kernel(DevState* state, float beta1, float beta2) {
     state->iter = 0u;
     state->vpt_pass = 0u;
+    state->wide_far_refs = kWideFarRefs;
     set_bias_corrections(state, beta1, beta2);
 }
 
@@ -469,6 +470,13 @@ __global__ void advance_state_kernel(DevState* state, uint32_t vpt_passes, float
 
 void launch_reset_state(DevState* state, float beta1, float beta2, cudaStream_t st) {
     reset_state_kernel<<<1, 1, 0, st>>>(state, beta1, beta2);
+    note_launches(1);
+}
+
+__global__ void set_wide_far_refs_kernel(DevState* state, int value) { state->wide_far_refs = value; }
+
+void launch_set_wide_far_refs(DevState* state, int value, cudaStream_t st) {
+    set_wide_far_refs_kernel<<<1, 1, 0, st>>>(state, value);
     note_launches(1);
 }
 

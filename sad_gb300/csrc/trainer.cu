@@ -409,6 +409,8 @@ static size_t carve_trainer(sad_trainer* t, void* base) {
     c.take(t->metric, 1);
     c.take(t->count, 4);
     c.take(t->state, 1);
+    if (base)
+        for (int b = 0; b < 3; ++b) t->tmap[b].wide_far_refs = &t->state->wide_far_refs;
     c.take(t->prune_k, static_cast<size_t>(std::max(1, t->cfg.iterations)));
     char* sort_temp = nullptr;
     c.take(sort_temp, radix_sort_temp_bytes(std::max<uint32_t>(t->cap, t->hpadded)));
@@ -601,6 +603,7 @@ extern "C" sad_status_t sad_trainer_init(sad_trainer_t* t, const float* sites_ho
     SAD_TRY(check_cuda(cudaMemsetAsync(t->stats_fix, 0, static_cast<size_t>(t->cap) * 8 * sizeof(long long), s),
                        "trainer stats clear"));
     launch_reset_state(t->state, t->cfg.beta1, t->cfg.beta2, s);
+    t->tuner.reset(t->cfg.autotune != 0, t->cfg.cand_update_freq);
     t->n = n0;
     t->active = active;
     t->iter = 0;
@@ -647,8 +650,13 @@ extern "C" sad_status_t sad_trainer_run(sad_trainer_t* t, int end) {
     bool eager = !c.use_graphs || t->timing;
     t->tev_used = 0;
     NvtxRange r_run(eager ? "fit iterations (eager)" : "fit iterations (graph replays)");
+    struct EndRun {  // the autotuner drops windows that did not close in this call
+        ShapeTuner& tuner;
+        ~EndRun() { tuner.end_run(); }
+    } end_run{t->tuner};
     for (int it = t->iter; it < end; ++it) {
         const IterPlan& p = t->plan[it];
+        SAD_TRY(check_cuda(t->tuner.before_iteration(t->plan, t->state, it, end, t->st), "trainer autotuner"));
         if (p.upd && use_h && (!t->hilbert_ready || t->hilbert_count != t->n))
             SAD_TRY(build_hilbert(t, t->st));
         if (p.dens) {
@@ -765,6 +773,8 @@ extern "C" sad_status_t sad_trainer_info(sad_trainer_t* t, sad_trainer_info_t* i
     info->gpu_ms_gradients = t->grad_ms;
     info->gradient_launches = t->grad_launches;
     info->kernel_launches = sad_launch_count();
+    info->wide_far_refs = t->tuner.rule();
+    info->tune_rounds = t->tuner.rounds();
     return SAD_OK;
 }
 

@@ -9,6 +9,7 @@
 #include "common.cuh"
 #include "host_common.h"
 #include "kernels.h"
+#include "tuner.h"
 
 namespace sad {
 
@@ -89,6 +90,7 @@ struct sad_trainer {
     size_t tev_used = 0;
     double grad_ms = 0.0;
     int grad_launches = 0;
+    sad::ShapeTuner tuner;  // tile-table shape rule, tuned while the fit runs
     std::chrono::steady_clock::time_point t0;
 };
 

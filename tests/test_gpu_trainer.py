@@ -131,3 +131,41 @@ def test_render_from_sites_matches_oracle_pipeline(cuda, orc, w, h, n):
     # 16 chained candidate passes: a near-tie resolved differently can propagate, so the
     # check is on the rendered image
     assert diff.mean() < 2e-4 and np.percentile(diff, 99.9) < 1e-2, (diff.mean(), diff.max())
+
+
+def _tuned_fit(img, cfg, chunks=None):
+    from sad_gb300.trainer import Trainer
+    h, w = img.shape[:2]
+    with Trainer(w, h, cfg) as tr:
+        tr.set_target(img)
+        tr.init()
+        for end in (chunks or []):
+            tr.run(end)
+        tr.run()
+        return tr.sites(active_only=False), tr.info()
+
+
+def test_autotuner_leaves_the_fit_bit_identical(cuda):
+    """The tile-table shape autotuner switches the registration's rule between refresh
+    windows while it times them; every rule gives the same fixed-point sums, so a tuned fit
+    equals an untuned one bit for bit.  Dense sites (5000 on 128x96) put far entries in
+    many tiles, so the arms give tiles different shapes."""
+    img = cases.scene(128, 96, 9)[0]
+    cfg = dict(n_sites=5000, max_sites=5000, iterations=200, prune_percentile=0.0)
+    fixed, info0 = _tuned_fit(img, small_cfg(autotune=0, **cfg))
+    tuned, info1 = _tuned_fit(img, small_cfg(autotune=1, **cfg))
+    assert info0.tune_rounds == 0 and info0.wide_far_refs == 256
+    assert info1.tune_rounds == 1  # one round: 8 clean windows from the second refresh
+    assert info1.wide_far_refs in (64, 256, 1024, 1 << 29)
+    np.testing.assert_array_equal(tuned, fixed)
+    # the same in several run calls (windows that would span a call boundary are not timed)
+    # and in eager mode, and with prune steps that the timed windows skip
+    chunked, info2 = _tuned_fit(img, small_cfg(autotune=1, **cfg), chunks=[37, 90, 91, 150])
+    np.testing.assert_array_equal(chunked, fixed)
+    assert info2.tune_rounds == 1
+    eager, _ = _tuned_fit(img, small_cfg(autotune=1, use_graphs=0, **cfg))
+    np.testing.assert_array_equal(eager, fixed)
+    pruned = dict(cfg, prune_percentile=0.02, prune_start=20, prune_freq=30, prune_end=180)
+    a, _ = _tuned_fit(img, small_cfg(autotune=0, **pruned))
+    b, _ = _tuned_fit(img, small_cfg(autotune=1, **pruned))
+    np.testing.assert_array_equal(a, b)
