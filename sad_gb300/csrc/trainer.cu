@@ -57,6 +57,11 @@ static void drop_graphs(sad_trainer* t) {
                     cudaGraphExecDestroy(g);
                     g = nullptr;
                 }
+    for (auto& g : t->wgraphs)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
 }
 
 // Host plan of the whole schedule (the same decisions the reference makes at run time).
@@ -303,6 +308,39 @@ static sad_status_t capture_variant(sad_trainer* t, bool upd, bool prune, int fi
     e = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     return check_cuda(e, "trainer graph instantiate");
+}
+
+// A refresh window of cand_update_freq iterations from field `field`, captured whole.
+static sad_status_t capture_window(sad_trainer* t, int field, cudaGraphExec_t* out, uint64_t* kernels) {
+    cudaGraph_t graph = nullptr;
+    SAD_TRY(check_cuda(cudaStreamBeginCapture(t->st, cudaStreamCaptureModeThreadLocal),
+                       "trainer graph capture"));
+    const uint64_t before = sad_launch_count();
+    int f = field;
+    for (int k = 0; k < t->cfg.cand_update_freq; ++k)
+        f = iteration_body(t, k == 0, false, f, k == 0 ? t->passes : 0, t->st);
+    *kernels = sad_launch_count() - before;
+    unnote_launches(*kernels);
+    cudaError_t e = cudaStreamEndCapture(t->st, &graph);
+    if (e != cudaSuccess) return check_cuda(e, "trainer graph capture end");
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    return check_cuda(e, "trainer graph instantiate");
+}
+
+// Whether iterations [it, it + cand_update_freq) form a window that one captured replay
+// can run: a refresh first, then only plain iterations, all inside this run call, with no
+// log line due and the autotuner (which acts between iterations) off.
+static bool window_at(const sad_trainer* t, int it, int end) {
+    const sad_train_config_t& c = t->cfg;
+    const int len = c.cand_update_freq;
+    if (len < 2 || it + len > end || c.autotune) return false;
+    for (int k = 0; k < len; ++k) {
+        const IterPlan& p = t->plan[it + k];
+        if ((k == 0) != (p.upd != 0) || p.dens || p.prune) return false;
+        if (c.log_freq > 0 && ((it + k) % c.log_freq == 0 || it + k == c.iterations - 1)) return false;
+    }
+    return true;
 }
 
 static sad_status_t log_iteration(sad_trainer* t, int it) {
@@ -656,6 +694,19 @@ extern "C" sad_status_t sad_trainer_run(sad_trainer_t* t, int end) {
     } end_run{t->tuner};
     for (int it = t->iter; it < end; ++it) {
         const IterPlan& p = t->plan[it];
+        if (!eager && window_at(t, it, end)) {
+            if (use_h && (!t->hilbert_ready || t->hilbert_count != t->n)) SAD_TRY(build_hilbert(t, t->st));
+            cudaGraphExec_t& g = t->wgraphs[t->cur];
+            uint64_t& nk = t->wgraph_kernels[t->cur];
+            if (!g) SAD_TRY(capture_window(t, t->cur, &g, &nk));
+            SAD_TRY(check_cuda(cudaGraphLaunch(g, t->st), "trainer graph launch"));
+            note_launches(nk);
+            t->cur = refresh_target(t, t->cur);
+            SAD_TRY(check_launch("sad_trainer_run"));
+            it += c.cand_update_freq - 1;
+            t->iter = it + 1;
+            continue;
+        }
         SAD_TRY(check_cuda(t->tuner.before_iteration(t->plan, t->state, it, end, t->st), "trainer autotuner"));
         if (p.upd && use_h && (!t->hilbert_ready || t->hilbert_count != t->n))
             SAD_TRY(build_hilbert(t, t->st));

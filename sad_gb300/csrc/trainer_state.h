@@ -85,6 +85,11 @@ struct sad_trainer {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaGraphExec_t graphs[2][2][3] = {};
     uint64_t graph_kernels[2][2][3] = {};  // kernel launches one replay runs
+    // a whole refresh window (a refresh iteration and the iterations up to the next one, no
+    // densify or prune step) per start field: one replay, and programmatic dependent launch
+    // across its iteration boundaries
+    cudaGraphExec_t wgraphs[3] = {};
+    uint64_t wgraph_kernels[3] = {};
     bool timing = false;
     std::vector<cudaEvent_t> tev;
     size_t tev_used = 0;
