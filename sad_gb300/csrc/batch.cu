@@ -52,6 +52,8 @@ struct sad_batch {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_done = nullptr;
     cudaGraphExec_t graphs[2][2][3] = {};
     uint64_t graph_kernels[2][2][3] = {};  // kernel launches one replay runs
+    cudaGraphExec_t wgraphs[3] = {};  // a whole refresh window per start field (as the trainer's)
+    uint64_t wgraph_kernels[3] = {};
     std::vector<cudaEvent_t> tev;
     size_t tev_used = 0;
 };
@@ -66,6 +68,11 @@ void drop_batch_graphs(sad_batch* b) {
                     cudaGraphExecDestroy(g);
                     g = nullptr;
                 }
+    for (auto& g : b->wgraphs)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
 }
 
 uint32_t tiles_of(const sad_trainer* t) { return static_cast<uint32_t>(((t->w + 15) / 16) * ((t->h + 15) / 16)); }
@@ -247,6 +254,32 @@ void batch_iteration(sad_batch* b, bool upd, bool prune, int field, cudaStream_t
     launch_advance_state_batch(b->site_items, B, upd ? 1u : 0u, c.beta1, c.beta2, s);
 }
 
+// A refresh window (cand_update_freq iterations: the refresh, then plain ones) captured whole.
+sad_status_t capture_batch_window(sad_batch* b, int field, cudaGraphExec_t* out, uint64_t* kernels) {
+    cudaGraph_t graph = nullptr;
+    SAD_TRY(check_cuda(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal), "batch graph capture"));
+    const uint64_t before = sad_launch_count();
+    for (int k = 0; k < b->cfg.cand_update_freq; ++k)
+        batch_iteration(b, k == 0, false, k == 0 ? field : refresh_target_field(1, field), b->st);
+    *kernels = sad_launch_count() - before;
+    unnote_launches(*kernels);
+    cudaError_t e = cudaStreamEndCapture(b->st, &graph);
+    if (e != cudaSuccess) return check_cuda(e, "batch graph capture end");
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    return check_cuda(e, "batch graph instantiate");
+}
+
+// Whether iterations [it, it + cand_update_freq) are a refresh window without a prune step
+// inside this run call (the images share one schedule).
+bool batch_window_at(const sad_batch* b, const std::vector<IterPlan>& plan, int it, int end) {
+    const int len = b->cfg.cand_update_freq;
+    if (len < 2 || it + len > end) return false;
+    for (int k = 0; k < len; ++k)
+        if ((k == 0) != (plan[it + k].upd != 0) || plan[it + k].prune || plan[it + k].dens) return false;
+    return true;
+}
+
 sad_status_t capture_batch(sad_batch* b, bool upd, bool prune, int field, cudaGraphExec_t* out, uint64_t* kernels) {
     cudaGraph_t graph = nullptr;
     SAD_TRY(check_cuda(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal), "batch graph capture"));
@@ -376,6 +409,18 @@ extern "C" sad_status_t sad_batch_run(sad_batch_t* b, int end) {
     NvtxRange r(eager ? "batch iterations (eager)" : "batch iterations (graph replays)");
     for (int it = b->iter; it < end; ++it) {
         const IterPlan& p = plan[it];
+        if (!eager && batch_window_at(b, plan, it, end)) {
+            cudaGraphExec_t& g = b->wgraphs[b->cur];
+            uint64_t& nk = b->wgraph_kernels[b->cur];
+            if (!g) SAD_TRY(capture_batch_window(b, b->cur, &g, &nk));
+            SAD_TRY(check_cuda(cudaGraphLaunch(g, b->st), "batch graph launch"));
+            note_launches(nk);
+            SAD_TRY(check_launch("sad_batch_run"));
+            b->cur = refresh_target_field(1, b->cur);
+            it += b->cfg.cand_update_freq - 1;
+            b->iter = it + 1;
+            continue;
+        }
         if (eager) {
             batch_iteration(b, p.upd, p.prune, b->cur, b->st);
         } else {
