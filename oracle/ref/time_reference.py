@@ -37,6 +37,7 @@ def run_reference(png: str, repeats: int, log_freq: int):
     exe = REF_EXE
     cwd = os.path.join(ROOT, "baseline", "_ref", "sad")
     best = None
+    runs = []  # (final PSNR line, last logged PSNR with two decimals) of every repeat
     for _ in range(repeats):
         out_dir = tempfile.mkdtemp()
         t0 = time.perf_counter()
@@ -49,11 +50,16 @@ def run_reference(png: str, repeats: int, log_freq: int):
         psnr = re.findall(r"Final PSNR: ([0-9.]+)", r.stdout)
         ttime = re.findall(r"Training time: ([0-9.]+) s", r.stdout)
         act = re.findall(r"Active: (\d+)/(\d+)", r.stdout)
+        logged = re.findall(r"Iter\s+(\d+) \| PSNR: ([0-9.]+) dB", r.stdout)
+        runs.append((float(psnr[-1]) if psnr else None,
+                     (int(logged[-1][0]), float(logged[-1][1])) if logged else None))
         res = {"it_per_s": its[-1] if its else None, "psnr_db": float(psnr[-1]) if psnr else None,
                "training_time_s": float(ttime[-1]) if ttime else None, "wall_s": round(wall, 3),
                "active_final": int(act[-1][0]) if act else None, "log": r.stdout.splitlines()[-12:]}
         if best is None or (res["it_per_s"] or 0) > (best["it_per_s"] or 0):
             best = res
+    best["psnr_runs"] = [r[0] for r in runs]
+    best["last_log_psnr_runs"] = [r[1] for r in runs]  # [iteration, PSNR] of the last log line
     return best
 
 
