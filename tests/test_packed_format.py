@@ -2,11 +2,15 @@
 backends/metal/sources/utils/packed_inference.swift:86-199, decode
 backends/metal/shaders/sad_common.metal:71-120, render packed_render_encoder.metal:3-31).
 
-The reference's packer is Swift and its decoder a Metal shader; neither runs here, so the
-oracle restatement (oracle/sad_oracle.c) is pinned by known-answer words worked out by hand
-from the format, and by round-trip bounds.  The CUDA kernels are compared with the oracle:
-every word bit-exact except the direction angle, which may differ by one step where
-atan2f's last bit differs; the decode is exact except cos/sin of the angle."""
+The reference's packer is Swift and does not run here.  Its decoder is a Metal function
+that compiles as plain C++ under a shim of the Metal types: tests/golden/packed_decode.npz
+holds the words of the oracle's packer (oracle/sad_oracle.c) decoded by the reference's own
+decodePackedSite (tests/golden/make_packed_fixture.py).  So the decode is pinned to the
+reference bit for bit, the packer to the reference's decoder by round-trip bounds, and both
+also by known-answer words worked out by hand from the format.  The CUDA kernels are
+compared with the oracle and the fixture: every word bit-exact except the direction angle,
+which may differ by one step where atan2f's last bit differs; the decode is exact except
+cos/sin of the angle."""
 import ctypes as C
 
 import numpy as np
@@ -94,6 +98,53 @@ def test_round_trip_bounds():
     assert np.all((packed[~act, 0] >> 30) & 1) and not np.any((packed[act, 0] >> 30) & 1)
 
 
+def _fixture_cases():
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "packed_decode.npz"))
+    for c in ("a", "b", "edges", "one"):
+        w, h = (int(v) for v in z[f"{c}_size"])
+        yield (c, z[f"{c}_sites"], z[f"{c}_words"], z[f"{c}_quant"], w, h, z[f"{c}_decoded"],
+               z[f"{c}_active"].astype(bool))
+
+
+EXACT = [0, 1, 2, 3, 4, 5, 6, 9]  # every decoded field but the direction (cos/sin of the angle)
+
+
+def test_oracle_decode_matches_reference_decoder():
+    """The oracle's unpack against the reference's decodePackedSite on the same words:
+    bit-exact (the direction within 2 ulps, for another host's libm); inactive sites by the
+    decoder's flag."""
+    for c, sites, words, quant, w, h, ref, act in _fixture_cases():
+        np.testing.assert_array_equal(words, orc.pack_inference_sites(sites, w, h)[0])  # packer unchanged
+        u = orc.unpack_inference_sites(words, quant, w, h)
+        np.testing.assert_array_equal(u[act][:, EXACT].view(np.uint32), ref[act][:, EXACT].view(np.uint32), err_msg=c)
+        ulp = np.abs(u[act][:, 7:9].view(np.int32).astype(np.int64) - ref[act][:, 7:9].view(np.int32).astype(np.int64))
+        assert ulp.size == 0 or ulp.max() <= 2, c
+        assert np.all(u[~act, :2] == -1.0), c
+
+
+def test_packer_round_trip_through_reference_decoder():
+    """The oracle packer's words, decoded by the reference's decoder, give back every active
+    site within half a quantisation step per field (an angle step for the direction, f16
+    for log_aniso), and the decoder reads inactive sites as inactive."""
+    for c, sites, words, quant, w, h, ref, act in _fixture_cases():
+        want_act = (sites[:, 0] >= 0) & (sites[:, 1] >= 0)
+        np.testing.assert_array_equal(act, want_act, err_msg=c)
+        a, u = sites[act], ref[act]
+        if not len(a):
+            continue
+        step = lambda scale, levels: scale / levels / 2 + 1e-6 * max(1.0, scale)  # noqa: E731
+        err = np.abs(u - a)
+        assert err[:, 0].max() <= step(w - 1, 32767) and err[:, 1].max() <= step(h - 1, 32767), c
+        for k, (qs, levels) in enumerate([(quant[1], 65535), (quant[3], 65535), (quant[5], 2047),
+                                          (quant[7], 2047), (quant[9], 1023)]):
+            assert err[:, 2 + k].max() <= step(qs, levels), (c, k)
+        ang = np.arctan2(a[:, 8], a[:, 7])
+        dang = np.angle(np.exp(1j * (np.arctan2(u[:, 8], u[:, 7]) - ang)))
+        assert np.abs(dang).max() <= np.pi / 65535 + 1e-5, c
+        np.testing.assert_array_equal(u[:, 9], a[:, 9].astype(np.float16).astype(np.float32), err_msg=c)
+
+
 def test_degenerate_sets():
     s = random_sites(10, W, H, seed=1, inactive_every=1)  # all inactive
     packed, quant = orc.pack_inference_sites(s, W, H)
@@ -162,6 +213,20 @@ def test_gpu_pack_matches_oracle(sadlib, cuda, n, w, h):
     uo = orc.unpack_inference_sites(want, wq, w, h)
     np.testing.assert_array_equal(u[:, [0, 1, 2, 3, 4, 5, 6, 9]], uo[:, [0, 1, 2, 3, 4, 5, 6, 9]])
     np.testing.assert_allclose(u[:, 7:9], uo[:, 7:9], rtol=0, atol=4e-7)
+
+
+@pytest.mark.gpu
+def test_gpu_unpack_matches_reference_decoder(sadlib, cuda):
+    """The CUDA unpack kernel on the fixture's words against the reference's decoder:
+    bit-exact except the direction (CUDA cosf/sinf, within 4e-7)."""
+    for c, sites, words, quant, w, h, ref, act in _fixture_cases():
+        u = _gpu_unpack(sadlib, words, quant, w, h)
+        np.testing.assert_array_equal(u[act][:, EXACT].view(np.uint32), ref[act][:, EXACT].view(np.uint32), err_msg=c)
+        np.testing.assert_allclose(u[act][:, 7:9], ref[act][:, 7:9], rtol=0, atol=4e-7, err_msg=c)
+        assert np.all(u[~act, :2] == -1.0), c
+        got, gq = _gpu_pack(sadlib, sites, w, h)
+        np.testing.assert_array_equal(gq, quant)
+        _assert_words_match(got, words)
 
 
 @pytest.mark.gpu
