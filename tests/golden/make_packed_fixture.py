@@ -6,7 +6,8 @@ The decoder compiles as plain C++ under a shim of the Metal types (oracle/ref/me
 oracle/ref/metal_decode.py, built from the reference checkout).  This script packs seeded
 site sets with the oracle's restatement of the packer, decodes the words with the
 reference's decoder and writes tests/golden/packed_decode.npz: sites, words, quant,
-width, height, decoded sites [n,10] and the decoder's active flags.
+width, height, decoded sites [n,10] and the decoder's active flags; and, for one small
+image, the reference's packed render (computePackedWeights) of a candidate field.
 
     python tests/golden/make_packed_fixture.py /path/to/reference
 """
@@ -39,6 +40,19 @@ def reference_decode(lib, words, quant, w, h):
     return out, act
 
 
+def reference_render(lib, words, quant, c0, c1, inv_s2, w, h):
+    rgb = np.zeros((h, w, 3), np.float32)
+    f = lib.ref_render_packed
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_void_p]
+    words = np.ascontiguousarray(words, np.uint32)
+    quant = np.ascontiguousarray(quant, np.float32)
+    c0 = np.ascontiguousarray(c0, np.uint32)
+    c1 = np.ascontiguousarray(c1, np.uint32)
+    f(words.ctypes.data, quant.ctypes.data, words.shape[0], c0.ctypes.data, c1.ctypes.data, inv_s2, w, h,
+      rgb.ctypes.data)
+    return rgb
+
+
 def main(reference_root: str) -> None:
     lib = C.CDLL(metal_decode.build(reference_root))
     cases = {}
@@ -66,6 +80,22 @@ def main(reference_root: str) -> None:
         out[f"{name}_size"] = np.int32([w, h])
         out[f"{name}_decoded"] = dec
         out[f"{name}_active"] = act
+    # the packed render (renderVoronoiPacked's softmax over the candidates) of a 64x48 image:
+    # nearest-site candidate lists with an out-of-range id, a repeated id and an inactive
+    # site among them
+    import cases as scenes
+    w, h, n = 64, 48, 200
+    _, sites = scenes.scene(w, h, n, 5)
+    sites[::7, 0:2] = -1.0
+    words, quant = orc.pack_inference_sites(sites, w, h)
+    c0, c1 = scenes.knn_field(sites, w, h)
+    c1 = c1.copy()
+    c1[::5, 3] = n + 7
+    c1[1::5, 2] = c0[1::5, 0]
+    inv_s2 = np.float32(1.0 / max(w, h) ** 2)
+    out.update(render_words=words, render_quant=quant, render_c0=c0, render_c1=c1,
+               render_size=np.int32([w, h]), render_inv_s2=np.float32([inv_s2]),
+               render_rgb=reference_render(lib, words, quant, c0, c1, inv_s2, w, h))
     np.savez_compressed(os.path.join(HERE, "packed_decode.npz"), **out)
     print("wrote", os.path.join(HERE, "packed_decode.npz"), sorted(cases))
 

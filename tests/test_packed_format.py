@@ -5,9 +5,10 @@ backends/metal/shaders/sad_common.metal:71-120, render packed_render_encoder.met
 The reference's packer is Swift and does not run here.  Its decoder is a Metal function
 that compiles as plain C++ under a shim of the Metal types: tests/golden/packed_decode.npz
 holds the words of the oracle's packer (oracle/sad_oracle.c) decoded by the reference's own
-decodePackedSite (tests/golden/make_packed_fixture.py).  So the decode is pinned to the
-reference bit for bit, the packer to the reference's decoder by round-trip bounds, and both
-also by known-answer words worked out by hand from the format.  The CUDA kernels are
+decodePackedSite (tests/golden/make_packed_fixture.py), and the reference's packed render
+(computePackedWeights) of one small image.  So the decode and the render are pinned to the
+reference, the packer to the reference's decoder by round-trip bounds, and both also by
+known-answer words worked out by hand from the format.  The CUDA kernels are
 compared with the oracle and the fixture: every word bit-exact except the direction angle,
 which may differ by one step where atan2f's last bit differs; the decode is exact except
 cos/sin of the angle."""
@@ -145,6 +146,24 @@ def test_packer_round_trip_through_reference_decoder():
         np.testing.assert_array_equal(u[:, 9], a[:, 9].astype(np.float16).astype(np.float32), err_msg=c)
 
 
+def _render_case():
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "packed_decode.npz"))
+    w, h = (int(v) for v in z["render_size"])
+    return (z["render_words"], z["render_quant"], z["render_c0"], z["render_c1"], float(z["render_inv_s2"][0]),
+            w, h, z["render_rgb"])
+
+
+def test_oracle_render_matches_reference_packed_render():
+    """The oracle's render of its decoded sites against the reference's packed render
+    (computePackedWeights of renderVoronoiPacked) of the same words and candidate field:
+    equal here; 1e-6 allows another host's libm."""
+    words, quant, c0, c1, inv_s2, w, h, want = _render_case()
+    dec = orc.unpack_inference_sites(words, quant, w, h)
+    got = orc.render(c0, c1, dec, w, h, inv_s2=inv_s2)
+    assert np.max(np.abs(got - want)) <= 1e-6
+
+
 def test_degenerate_sets():
     s = random_sites(10, W, H, seed=1, inactive_every=1)  # all inactive
     packed, quant = orc.pack_inference_sites(s, W, H)
@@ -227,6 +246,22 @@ def test_gpu_unpack_matches_reference_decoder(sadlib, cuda):
         got, gq = _gpu_pack(sadlib, sites, w, h)
         np.testing.assert_array_equal(gq, quant)
         _assert_words_match(got, words)
+
+
+@pytest.mark.gpu
+def test_gpu_render_packed_matches_reference(sadlib, cuda):
+    """The CUDA packed render against the reference's packed render of the same words and
+    candidate field (CUDA expf/cosf/sinf: the render tolerance, 1e-4)."""
+    import torch
+    words, quant, c0, c1, inv_s2, w, h, want = _render_case()
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).cuda()  # noqa: E731
+    dc0, dc1, dp = t(c0), t(c1), t(words)
+    dq = torch.from_numpy(quant).cuda()
+    out = torch.zeros((h, w, 3), device="cuda")
+    assert sadlib.sad_render_packed(_ptr(dc0), _ptr(dc1), _ptr(out), _ptr(dp), _ptr(dq), inv_s2, words.shape[0],
+                                    w, h, w, h, None) == 0
+    torch.cuda.synchronize()
+    assert np.max(np.abs(out.cpu().numpy() - want)) <= 1e-4
 
 
 @pytest.mark.gpu
