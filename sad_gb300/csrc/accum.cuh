@@ -380,10 +380,14 @@ __device__ __forceinline__ void write_tile_keys(const Table& table, int tid, int
 }
 
 #ifdef __CUDACC__
-// Opt a kernel into more than 48 KB of dynamic shared memory (a no-op below that).
+// Opt a kernel into `bytes` of dynamic shared memory when that and its static shared
+// memory exceed the default 48 KB per block (a no-op below that).
 template <class Kernel>
 inline cudaError_t allow_dynamic_smem(Kernel kernel, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
+    cudaFuncAttributes a{};
+    cudaError_t e = cudaFuncGetAttributes(&a, kernel);
+    if (e != cudaSuccess) return e;
+    if (bytes + a.sharedSizeBytes <= 48 * 1024) return cudaSuccess;
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(bytes));
 }
