@@ -193,6 +193,9 @@ def run_ours(args):
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": prof.get("dram_bytes_per_launch"),
                 "limiter": prof.get("limiter"),
+                # the bound the kernel does meet: L1 data-pipe wavefronts and issue, as fractions
+                # of their peaks in the committed ncu capture (HBM stays at ~10%)
+                "limiter_pct_of_peak": prof.get("limiter_pct_of_peak"),
                 "kernel": prof.get("kernel", "fused_gradients_pre_kernel"), "launch_ms": round(grad_ms, 5),
                 "algorithmic_bytes_per_launch": alg_bytes,
                 "algorithmic_bytes_active_weighted": int(alg_active),
