@@ -529,6 +529,34 @@ def serve_sweep(args, rates, workers, budget, fit_cfg, fit_imgs, max_fits):
     return rows
 
 
+def run_profile_batch(args):
+    """The batch workload as one lockstep batch, for ncu: graph replays up to
+    --profile-iters, then --profile-window eager iterations (every kernel its own launch)
+    inside the NVTX range "late" (select them with ncu --nvtx --nvtx-include "late/");
+    nothing is timed.  With --profile-window 0 every iteration runs eager."""
+    import torch
+    from sad_gb300.batch import Batch
+    from sad_gb300.config import train_config
+    torch.cuda.set_device(0)
+    imgs = batch_images(args.batch_images)
+    window = args.profile_window
+    cfg = train_config(log_freq=0, iterations=args.batch_iters, use_graphs=1 if window > 0 else 0)
+    with Batch([(i.shape[1], i.shape[0]) for i in imgs], config=cfg) as b:
+        for i, img in enumerate(imgs):
+            b.set_target(i, img)
+        b.init()
+        b.run(args.profile_iters)
+        b.synchronize()
+        if window > 0:
+            b.enable_timing(True)  # eager launches from here on
+            torch.cuda.nvtx.range_push("late")
+            b.run(min(args.batch_iters, args.profile_iters + window))
+            b.synchronize()
+            torch.cuda.nvtx.range_pop()
+    print(json.dumps({"mode": "profile", "workload": "batch", "iterations": args.profile_iters,
+                      "window": window}))
+
+
 def run_profile(args):
     """Eager (graph-free) fit of the workload for `--profile-iters` iterations, so every
     kernel is a separate launch for ncu; nothing is timed.  --profile-sites N fits N sites
@@ -562,6 +590,8 @@ def main():
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     ap.add_argument("--profile-iters", type=int, default=200)
     ap.add_argument("--profile-sites", type=int, default=0)
+    ap.add_argument("--profile-window", type=int, default=0,
+                    help="profile mode, batch workload: eager iterations after --profile-iters")
     ap.add_argument("--workload", default="fit", choices=["fit", "batch", "serve"],
                     help="fit: the 1024x1024 headline fit; batch: 64 mixed-size fits through the "
                          "executor; serve: the Poisson render/fit mix")
@@ -580,7 +610,7 @@ def main():
                     help="also run the same request streams with one worker (requests one at a time)")
     args = ap.parse_args()
     if args.mode == "profile":
-        run_profile(args)
+        run_profile_batch(args) if args.workload == "batch" else run_profile(args)
         return
     if args.workload != "fit":
         if args.impl == "reference":
