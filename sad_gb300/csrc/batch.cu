@@ -42,11 +42,13 @@ struct sad_batch {
     // device tables, one allocation
     void* tables = nullptr;
     SiteBatchItem* site_items = nullptr;
-    GradBatchItem* grad_items[3] = {};
-    RegisterBatchItem* reg_items[3] = {};
-    VptBatchItem* vpt_items[3] = {};
-    uint32_t* tile_prefix = nullptr;
-    uint32_t* vpt_prefix = nullptr;
+    // the per-pixel kernels' images and block prefixes stay on the host: those kernels take
+    // them as kernel parameters (BatchArgs; captured by value, and the graphs are dropped
+    // whenever the tables change)
+    std::vector<GradBatchItem> grad_items[3];
+    std::vector<RegisterBatchItem> reg_items[3];
+    std::vector<VptBatchItem> vpt_items[3];
+    std::vector<uint32_t> tile_prefix, vpt_prefix;
     uint32_t* site_prefix = nullptr;
     cudaStream_t st = nullptr, side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_done = nullptr;
@@ -182,9 +184,7 @@ sad_status_t build_tables(sad_batch* b) {
     b->site_grid = static_cast<uint32_t>(std::min<uint64_t>(std::max<uint64_t>(sum_n, 1), 152ull * 8 * 256));
 
     auto a256 = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t bytes = a256(B * sizeof(SiteBatchItem)) + 3 * a256(B * sizeof(GradBatchItem)) +
-                         3 * a256(B * sizeof(RegisterBatchItem)) + 3 * a256(B * sizeof(VptBatchItem)) +
-                         3 * a256((B + 1) * sizeof(uint32_t));
+    const size_t bytes = a256(B * sizeof(SiteBatchItem)) + a256((B + 1) * sizeof(uint32_t));
     if (!b->tables) SAD_TRY(check_cuda(cudaMalloc(&b->tables, bytes), "sad_batch_init: table allocation"));
     char* base = static_cast<char*>(b->tables);
     std::vector<char> host(bytes, 0);
@@ -195,12 +195,14 @@ sad_status_t build_tables(sad_batch* b) {
         off += a256(n);
     };
     put(b->site_items, site.data(), B * sizeof(SiteBatchItem));
-    for (int f = 0; f < 3; ++f) put(b->grad_items[f], grad[f].data(), B * sizeof(GradBatchItem));
-    for (int f = 0; f < 3; ++f) put(b->reg_items[f], reg[f].data(), B * sizeof(RegisterBatchItem));
-    for (int f = 0; f < 3; ++f) put(b->vpt_items[f], vpt[f].data(), B * sizeof(VptBatchItem));
-    put(b->tile_prefix, tile_prefix.data(), (B + 1) * sizeof(uint32_t));
-    put(b->vpt_prefix, vpt_prefix.data(), (B + 1) * sizeof(uint32_t));
     put(b->site_prefix, tile_prefix.data(), (B + 1) * sizeof(uint32_t));  // rewritten on the device below
+    for (int f = 0; f < 3; ++f) {
+        b->grad_items[f] = grad[f];
+        b->reg_items[f] = reg[f];
+        b->vpt_items[f] = vpt[f];
+    }
+    b->tile_prefix = tile_prefix;
+    b->vpt_prefix = vpt_prefix;
     SAD_TRY(check_cuda(cudaMemcpyAsync(b->tables, host.data(), bytes, cudaMemcpyHostToDevice, b->st),
                        "sad_batch_init: table upload"));
     launch_batch_site_prefix(b->site_items, B, b->site_prefix, b->st);
@@ -218,15 +220,15 @@ void batch_iteration(sad_batch* b, bool upd, bool prune, int field, cudaStream_t
         cudaEventRecord(b->ev_fork, s);
         cudaStreamWaitEvent(b->side, b->ev_fork, 0);
         launch_pack_geom_batch(b->site_items, b->site_prefix, B, b->site_grid, b->side);
-        launch_vpt_batch(b->vpt_items[field], b->vpt_prefix, B, b->total_vpt, b->side);
-        launch_register_tiles_batch(b->reg_items[next], b->tile_prefix, B, b->total_tiles, b->side);
+        launch_vpt_batch(b->vpt_items[field].data(), b->vpt_prefix.data(), B, b->side);
+        launch_register_tiles_batch(b->reg_items[next].data(), b->tile_prefix.data(), B, b->side);
         cudaEventRecord(b->ev_join, b->side);
     }
     const bool timed = b->timing && b->tev_used + 2 <= b->tev.size();
     if (timed) cudaEventRecord(b->tev[b->tev_used], s);
     {
         NvtxRange r("batch: gradients");
-        launch_gradients_batch(b->grad_items[field], b->tile_prefix, B, b->total_tiles, prune, false, s);
+        launch_gradients_batch(b->grad_items[field].data(), b->tile_prefix.data(), B, prune, false, s);
     }
     if (timed) {
         cudaEventRecord(b->tev[b->tev_used + 1], s);

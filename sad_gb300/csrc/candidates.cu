@@ -316,39 +316,23 @@ __global__ void __launch_bounds__(256, 5) vpt_kernel(VptParams prm, Src src) {
 
 // Batched form over the 32x8-pixel blocks of every image of a batch (the trainer's
 // refresh pass on the f16-rounded geometry).
-__global__ void __launch_bounds__(256, 5) vpt_batch_kernel(const VptBatchItem* __restrict__ items,
-                                                           const uint32_t* __restrict__ block_prefix,
-                                                           uint32_t n_items) {
+__global__ void __launch_bounds__(256, 5) vpt_batch_kernel(const __grid_constant__ BatchArgs<VptBatchItem> a) {
     pdl_wait();
-    __shared__ VptParams s_p;
-    __shared__ const SiteGeom* s_g;
-    __shared__ int s_local, s_bx;
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    if (tid == 0) {
-        uint32_t lo = 0, hi = n_items;
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (__ldg(block_prefix + mid) <= blockIdx.x) lo = mid;
-            else hi = mid;
-        }
-        s_p = items[lo].p;
-        s_g = items[lo].vgeom;
-        s_bx = items[lo].blocks_x;
-        s_local = static_cast<int>(blockIdx.x - block_prefix[lo]);
-    }
-    __syncthreads();
-    const int x = (s_local % s_bx) * 32 + threadIdx.x;
-    const int y = (s_local / s_bx) * 8 + threadIdx.y;
-    if (x >= s_p.width || y >= s_p.height) return;
+    const uint32_t i = a.item_of(blockIdx.x);
+    const VptBatchItem& it = a.items[i];
+    const int local = static_cast<int>(blockIdx.x - a.block_prefix[i]);
+    const int x = (local % it.blocks_x) * 32 + threadIdx.x;
+    const int y = (local / it.blocks_x) * 8 + threadIdx.y;
+    if (x >= it.p.width || y >= it.p.height) return;
     uint32_t out[8];
-    vpt_pixel(s_p, PackedGeomSites{s_g}, x, y, out);
+    vpt_pixel(it.p, PackedGeomSites{it.vgeom}, x, y, out);
 }
 
-void launch_vpt_batch(const VptBatchItem* items, const uint32_t* block_prefix, uint32_t n_items,
-                      uint32_t total_blocks, cudaStream_t st) {
-    if (total_blocks == 0) return;
-    launch_pdl(vpt_batch_kernel, dim3(total_blocks), dim3(32, 8), 0, st, items, block_prefix, n_items);
-    note_launches(1);
+void launch_vpt_batch(const VptBatchItem* items, const uint32_t* block_prefix, uint32_t n_items, cudaStream_t st) {
+    for_each_batch_launch(items, block_prefix, n_items, [&](const BatchArgs<VptBatchItem>& a, uint32_t blocks) {
+        launch_pdl(vpt_batch_kernel, dim3(blocks), dim3(32, 8), 0, st, a);
+        note_launches(1);
+    });
 }
 
 static dim3 pixel_grid(int w, int h) { return dim3((w + 31) / 32, (h + 7) / 8); }

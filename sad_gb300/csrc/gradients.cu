@@ -341,38 +341,18 @@ __global__ void __launch_bounds__(256, 4) fused_gradients_pre_kernel(GradParams 
     grad_pre_tile<Src, kRemoval, kSSIM>(prm, src, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
-// Image of a batched launch's block: the last item whose first block is <= b (prefix[0]
-// = 0 and prefix[n_items] = the grid's block count).
-__device__ __forceinline__ uint32_t batch_item_of_block(const uint32_t* __restrict__ prefix, uint32_t items,
-                                                        uint32_t b) {
-    uint32_t lo = 0, hi = items;  // prefix[lo] <= b < prefix[hi]
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(prefix + mid) <= b) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// Batched form: one launch over the tiles of every image of a batch (tile_prefix[i] is the
-// first block of image i); each block copies its image's parameters into shared memory.
+// Batched form: one launch over the tiles of up to kBatchLaunchItems images, passed by
+// value.  Every thread finds its block's image in the constant bank, and grad_pre_tile
+// reads that image's parameters from there.
 template <class Src, bool kRemoval, bool kSSIM>
-__global__ void __launch_bounds__(256, 4) fused_gradients_batch_kernel(const GradBatchItem* __restrict__ items,
-                                                                       const uint32_t* __restrict__ tile_prefix,
-                                                                       uint32_t n_items) {
+__global__ void __launch_bounds__(256, 4)
+    fused_gradients_batch_kernel(const __grid_constant__ BatchArgs<GradBatchItem> a) {
     pdl_wait();
-    __shared__ GradParams s_prm;
-    __shared__ Src s_src;
-    __shared__ int s_local, s_tiles_x;
-    if (threadIdx.x == 0) {
-        const uint32_t i = batch_item_of_block(tile_prefix, n_items, blockIdx.x);
-        s_prm = items[i].p;
-        s_src = Src{items[i].geom, items[i].color};
-        s_tiles_x = items[i].tiles_x;
-        s_local = static_cast<int>(blockIdx.x - tile_prefix[i]);
-    }
-    __syncthreads();
-    grad_pre_tile<Src, kRemoval, kSSIM>(s_prm, s_src, s_local % s_tiles_x, s_local / s_tiles_x, s_tiles_x);
+    const uint32_t i = a.item_of(blockIdx.x);
+    const GradBatchItem& it = a.items[i];
+    const int local = static_cast<int>(blockIdx.x - a.block_prefix[i]);
+    grad_pre_tile<Src, kRemoval, kSSIM>(it.p, Src{it.geom, it.color}, local % it.tiles_x, local / it.tiles_x,
+                                        it.tiles_x);
 }
 
 template <class Src, bool kRemoval, bool kSSIM>
@@ -519,22 +499,16 @@ __global__ void __launch_bounds__(256) register_tiles_kernel(const uint4* __rest
     register_tile(c0, c1, n, w, h, cw, ch, map, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
-// Batched form over the tiles of every image of a batch.
-__global__ void __launch_bounds__(256) register_tiles_batch_kernel(const RegisterBatchItem* __restrict__ items,
-                                                                   const uint32_t* __restrict__ tile_prefix,
-                                                                   uint32_t n_items) {
+// Batched form over the tiles of up to kBatchLaunchItems images (by value, as the gradient
+// kernel's).
+__global__ void __launch_bounds__(256) register_tiles_batch_kernel(const __grid_constant__ BatchArgs<RegisterBatchItem> a) {
     pdl_wait();
-    __shared__ RegisterBatchItem s_it;
-    __shared__ int s_local;
-    if (threadIdx.x == 0) {
-        const uint32_t i = batch_item_of_block(tile_prefix, n_items, blockIdx.x);
-        s_it = items[i];
-        s_local = static_cast<int>(blockIdx.x - tile_prefix[i]);
-    }
-    __syncthreads();
-    const int tx = s_it.tiles_x;
-    register_tile(reinterpret_cast<const uint4*>(s_it.c0), reinterpret_cast<const uint4*>(s_it.c1), s_it.n, s_it.w,
-                  s_it.h, s_it.cw, s_it.ch, s_it.map, s_local % tx, s_local / tx, tx);
+    const uint32_t i = a.item_of(blockIdx.x);
+    const RegisterBatchItem& it = a.items[i];
+    const int local = static_cast<int>(blockIdx.x - a.block_prefix[i]);
+    const int tx = it.tiles_x;
+    register_tile(reinterpret_cast<const uint4*>(it.c0), reinterpret_cast<const uint4*>(it.c1), it.n, it.w, it.h,
+                  it.cw, it.ch, it.map, local % tx, local / tx, tx);
 }
 
 __device__ __forceinline__ void register_tile(const uint4* __restrict__ c0, const uint4* __restrict__ c1,
@@ -591,10 +565,11 @@ void launch_register_tiles(const uint32_t* c0, const uint32_t* c1, uint32_t n, i
 }
 
 void launch_register_tiles_batch(const RegisterBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
-                                 uint32_t total_tiles, cudaStream_t st) {
-    if (total_tiles == 0) return;
-    launch_pdl(register_tiles_batch_kernel, dim3(total_tiles), dim3(256), 0, st, items, tile_prefix, n_items);
-    note_launches(1);
+                                 cudaStream_t st) {
+    for_each_batch_launch(items, tile_prefix, n_items, [&](const BatchArgs<RegisterBatchItem>& a, uint32_t tiles) {
+        launch_pdl(register_tiles_batch_kernel, dim3(tiles), dim3(256), 0, st, a);
+        note_launches(1);
+    });
 }
 
 template <class Src, bool kFix, bool kRemoval, bool kSSIM>
@@ -678,25 +653,25 @@ void launch_gradients_prepared(const GradParams& p, const SiteGeom* geom, const 
 }
 
 template <bool kRemoval, bool kSSIM>
-static void launch_batch_variant(const GradBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
-                                 uint32_t total_tiles, cudaStream_t st) {
-    launch_pdl(fused_gradients_batch_kernel<PreparedSites, kRemoval, kSSIM>, dim3(total_tiles), dim3(256),
-               sizeof(typename GradLayout<true, kRemoval>::Pre), st, items, tile_prefix, n_items);
+static void launch_batch_variant(const BatchArgs<GradBatchItem>& a, uint32_t tiles, cudaStream_t st) {
+    launch_pdl(fused_gradients_batch_kernel<PreparedSites, kRemoval, kSSIM>, dim3(tiles), dim3(256),
+               sizeof(typename GradLayout<true, kRemoval>::Pre), st, a);
 }
 
 void launch_gradients_batch(const GradBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
-                            uint32_t total_tiles, bool removal, bool ssim, cudaStream_t st) {
-    if (total_tiles == 0) return;
+                            bool removal, bool ssim, cudaStream_t st) {
     ensure_gradient_kernels();
-    if (removal && ssim)
-        launch_batch_variant<true, true>(items, tile_prefix, n_items, total_tiles, st);
-    else if (removal)
-        launch_batch_variant<true, false>(items, tile_prefix, n_items, total_tiles, st);
-    else if (ssim)
-        launch_batch_variant<false, true>(items, tile_prefix, n_items, total_tiles, st);
-    else
-        launch_batch_variant<false, false>(items, tile_prefix, n_items, total_tiles, st);
-    note_launches(1);
+    for_each_batch_launch(items, tile_prefix, n_items, [&](const BatchArgs<GradBatchItem>& a, uint32_t tiles) {
+        if (removal && ssim)
+            launch_batch_variant<true, true>(a, tiles, st);
+        else if (removal)
+            launch_batch_variant<true, false>(a, tiles, st);
+        else if (ssim)
+            launch_batch_variant<false, true>(a, tiles, st);
+        else
+            launch_batch_variant<false, false>(a, tiles, st);
+        note_launches(1);
+    });
 }
 
 }  // namespace sad

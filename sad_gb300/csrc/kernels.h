@@ -11,6 +11,48 @@
 
 namespace sad {
 
+// Batched launches (one grid over the blocks of every image of a batch) take their images
+// by value: kernel parameters sit in the constant bank, so every block reads its image's
+// parameters through the constant cache (block-uniform and read-only, so neither copied
+// into shared memory nor aliased by the kernel's shared-memory stores and atomics).  One
+// launch covers up to kBatchLaunchItems images; block_prefix[i] is image i's first block
+// within the launch and block_prefix[n_items] the launch's block count.
+constexpr uint32_t kBatchLaunchItems = 96;
+template <class Item>
+struct BatchArgs {
+    uint32_t n_items;
+    uint32_t block_prefix[kBatchLaunchItems + 1];
+    Item items[kBatchLaunchItems];
+    // the image of block b: the last item whose first block is <= b
+    __device__ __forceinline__ uint32_t item_of(uint32_t b) const {
+        uint32_t lo = 0, hi = n_items;  // block_prefix[lo] <= b < block_prefix[hi]
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (block_prefix[mid] <= b) lo = mid;
+            else hi = mid;
+        }
+        return lo;
+    }
+};
+
+// Calls launch(args, blocks) for each run of up to kBatchLaunchItems images of the host
+// arrays items[n] and prefix[n + 1] (prefix[i]: image i's first block; prefix[0] = 0),
+// skipping runs without blocks.
+template <class Item, class Launch>
+inline void for_each_batch_launch(const Item* items, const uint32_t* prefix, uint32_t n, Launch&& launch) {
+    static_assert(sizeof(BatchArgs<Item>) <= 32000, "kernel parameters are limited to 32,764 bytes");
+    BatchArgs<Item> a;
+    for (uint32_t first = 0; first < n; first += kBatchLaunchItems) {
+        const uint32_t k = std::min(n - first, kBatchLaunchItems);
+        const uint32_t base = prefix[first], blocks = prefix[first + k] - base;
+        if (blocks == 0) continue;
+        a.n_items = k;
+        for (uint32_t i = 0; i <= k; ++i) a.block_prefix[i] = prefix[first + i] - base;
+        for (uint32_t i = 0; i < k; ++i) a.items[i] = items[first + i];
+        launch(a, blocks);
+    }
+}
+
 struct VptParams {
     const uint32_t* in0;
     const uint32_t* in1;
@@ -36,15 +78,14 @@ struct VptParams {
     uint32_t pow2, stages;
 };
 
-// Batched VPT pass: one grid over the 32x8 blocks of every image (block_prefix[i] is image
-// i's first block); items and prefix in device memory.
+// Batched VPT pass: one grid over the 32x8 blocks of every image (host arrays: items[n],
+// block_prefix[n + 1], image i's first block; BatchArgs).
 struct VptBatchItem {
     VptParams p;
     const SiteGeom* vgeom;
     int blocks_x;
 };
-void launch_vpt_batch(const VptBatchItem* items, const uint32_t* block_prefix, uint32_t n_items,
-                      uint32_t total_blocks, cudaStream_t st);
+void launch_vpt_batch(const VptBatchItem* items, const uint32_t* block_prefix, uint32_t n_items, cudaStream_t st);
 
 // render.cu
 void launch_prepare_sites(const Site* sites, SiteGeom* geom, SiteColor* color, uint32_t n,
@@ -118,8 +159,8 @@ struct TileMap {
     const int* wide_far_refs;  // device word with the tile-table shape rule (nullptr: kWideFarRefs)
 };
 // Batched launches: one grid over the tiles of every image of a batch; tile_prefix[i] is
-// image i's first block (tile_prefix[n_items] = total_tiles); items and prefixes live in
-// device memory.
+// image i's first block (tile_prefix[n_items] = total_tiles); host arrays, passed to the
+// kernels as BatchArgs.
 struct GradBatchItem {
     GradParams p;
     const SiteGeom* geom;
@@ -135,9 +176,9 @@ struct RegisterBatchItem {
     int tiles_x;
 };
 void launch_gradients_batch(const GradBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
-                            uint32_t total_tiles, bool removal, bool ssim, cudaStream_t st);
+                            bool removal, bool ssim, cudaStream_t st);
 void launch_register_tiles_batch(const RegisterBatchItem* items, const uint32_t* tile_prefix, uint32_t n_items,
-                                 uint32_t total_tiles, cudaStream_t st);
+                                 cudaStream_t st);
 size_t tile_map_words(int w, int h);  // u32 words of one TileMap (slot map + keys + counts)
 TileMap tile_map_at(uint32_t* base, int w, int h);
 void launch_register_tiles(const uint32_t* c0, const uint32_t* c1, uint32_t n, int w, int h,

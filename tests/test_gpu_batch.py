@@ -52,6 +52,26 @@ def test_batch_matches_single_fits_bitwise(cuda, graphs):
         assert (want_sites[:, 0] >= 0).sum() < CFG["n_sites"]  # the prune events ran
 
 
+def test_batch_of_more_images_than_one_launch_takes(cuda):
+    """The per-pixel stages take their images as kernel parameters, up to 96 per launch;
+    a larger batch runs each such stage as several launches, with the same results."""
+    from sad_gb300.batch import Batch
+    rng = np.random.default_rng(7)
+    sizes = [(int(rng.integers(16, 49)), int(rng.integers(16, 49))) for _ in range(100)]
+    imgs = [synthetic_image(w, h, seed=300 + i) for i, (w, h) in enumerate(sizes)]
+    cfg = dict(iterations=60, n_sites=300, max_sites=300, log_freq=0)
+    with Batch(sizes, **cfg) as b:
+        for i, img in enumerate(imgs):
+            b.set_target(i, img)
+        b.init()
+        b.run()
+        b.synchronize()
+        got = [b.sites(i, active_only=False) for i in range(len(imgs))]
+    for i in (0, 1, 47, 94, 95, 96, 97, 99):
+        want, _ = _solo(imgs[i], use_graphs=1, **cfg)
+        np.testing.assert_array_equal(got[i].view(np.uint32), want.view(np.uint32), err_msg=f"image {i}")
+
+
 def test_batch_timing_and_launch_count(cuda):
     from sad_gb300 import _lib
     from sad_gb300.batch import Batch
