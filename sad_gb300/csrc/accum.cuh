@@ -268,6 +268,68 @@ struct TileWords {
     }
 };
 
+// A third shape, for tiles of at most kLaneKeys entries (late in a fit most tiles hold
+// 10-30): one word per (entry, value, warp lane), shared by the block's eight warps, laid
+// over the same shared memory as TileWords.  The adds of one instruction then land in 32
+// banks, one per lane, and every lane may walk its candidates in the same order, which
+// makes the staged site records' loads broadcasts: in a late-fit ncu capture the L1/shared
+// pipe fell from 77% to 57% of its peak.  A word sums at most 8 terms (one pixel per warp; a
+// pixel adds to an entry once) of |x| < 2^22, so an entry's 32 lane words sum to less than
+// 2^30; a term of |v| >= 1/4 adds its low part here and its high part straight to the
+// site's global record (an exact integer add, like the flush).
+constexpr int kLaneKeys = 24;
+
+template <int NV>
+struct LaneWords {
+    int w[kLaneKeys][NV][32];
+
+    // zero the first `used` entries with the block's 256 threads
+    __device__ __forceinline__ void zero(int used, int tid) {
+        int4* p = reinterpret_cast<int4*>(&w[0][0][0]);
+        const int n = used * NV * 8;
+        for (int i = tid; i < n; i += 256) p[i] = make_int4(0, 0, 0, 0);
+    }
+    // lane `lane`'s terms for entry d (fix12: the [N][12] global records, dkey: the tile's
+    // keys by entry, for the high parts of large terms)
+    __device__ __forceinline__ void add(int d, int lane, const float (&v)[NV], long long* fix12,
+                                        const uint32_t* dkey) {
+        int* lw = &w[d][0][lane];
+        float m = 0.0f;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) m = fmaxf(m, fabsf(v[k]));
+        if (m < 0.25f) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                atomicAdd(lw + 32 * k, __float_as_int(fmaf(v[k], kFixScale, 12582912.0f)) - 0x4B400000);
+        } else {
+            long long* rec = fix12 + static_cast<size_t>(dkey[d]) * 12;
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                int h, l;
+                split_fix(v[k], h, l);
+                atomicAdd(lw + 32 * k, l);
+                if (h != 0) fix_add_global(rec + k, static_cast<long long>(h) * (1ll << kSplitLoBits));
+            }
+        }
+    }
+    // the block's flush: thread t sums the 32 lane words of (entry, value) pairs t, t + 256,
+    // ... in a bank-skewed order (lane l reads bank (j + l) & 31 at step j, so a warp's
+    // reads never conflict) and adds each nonzero sum to the site's global record
+    __device__ __forceinline__ void flush(int used, int tid, long long* fix12, const uint32_t* dkey) const {
+        const int lane = tid & 31, pairs = used * NV;
+        for (int q = tid; q < pairs; q += 256) {
+            const int* wq = &w[0][0][0] + q * 32;
+            int x = 0;
+#pragma unroll 8
+            for (int j = 0; j < 32; ++j) x += wq[(j + lane) & 31];
+            if (x != 0) {
+                const int d = q / NV, k = q - d * NV;
+                fix_add_global(fix12 + static_cast<size_t>(dkey[d]) * 12 + k, x);
+            }
+        }
+    }
+};
+
 // Keys and values of one tile (keys registered in the kernel).
 template <int NV, int SLOTS, class Mode>
 struct TileTable : KeyTable<SLOTS>, TileValues<NV, SLOTS, Mode> {

@@ -119,7 +119,10 @@ struct GradLayout {
     // precomputed registration (trainer): the tile's values, keys and staged sites, and
     // each thread's candidate weights (and removal deltas) for the accumulation loop
     struct Pre {
-        TileWords<NV> vals;  // lo words per pixel row (narrow tiles) or row parity (wide)
+        union {
+            TileWords<NV> vals;   // lo words per pixel row (narrow tiles) or row parity (wide)
+            LaneWords<NV> lanes;  // words per warp lane (tiles of at most kLaneKeys entries)
+        };
         uint32_t dkey[kTileKeys];
         // staged site records of the first kNarrowKeys entries (the entries of a wide tile
         // beyond them read their site from global memory)
@@ -129,6 +132,7 @@ struct GradLayout {
         float wts[kCand][256];
         float rem[kRemoval ? kCand : 1][256];
     };
+    static_assert(sizeof(LaneWords<NV>) <= sizeof(TileWords<NV>), "the lane words reuse the tile words' memory");
 };
 
 // Forward of one pixel: softmax over the 8 candidates, pred, dL/dpred (+ SSIM term) and,
@@ -366,12 +370,15 @@ __device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& 
     const bool wide = (tile_word & kTileWideFlag) != 0;  // uniform over the block
     // a narrow tile keeps its first kNarrowKeys entries; slot_of() sends the rest global
     const int used = wide ? tile_word & ~kTileWideFlag : min(tile_word, kNarrowKeys);
+    // the lane-word shape (uniform over the block; every shape gives the same sums)
+    const bool lanes = !wide && tile_word <= kLaneKeys;
+    if (lanes) sm.lanes.zero(used, tid);
     {
         const uint32_t* keys = prm.tile_keys + static_cast<size_t>(tile) * kTileKeys;
         for (int d = tid; d < used; d += 256) {
             const uint32_t key = keys[d];
             sm.dkey[d] = key;
-            sm.vals.zero(d, wide);
+            if (!lanes) sm.vals.zero(d, wide);
             if (d < kNarrowKeys) {
                 SiteGeom g;
                 float3 c;
@@ -443,8 +450,9 @@ __device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& 
         }
     }
 
-    // accumulate in a lane-rotated candidate order
-    const uint32_t r = lane_rotation();
+    // accumulate in a lane-rotated candidate order (spreads the row copies' adds over the
+    // banks), or with lane words in the same order in every lane (broadcast record loads)
+    const uint32_t r = lanes ? 0u : lane_rotation();
     const int rbits = TileWords<NV>::row_bits(lane >> 3, wide);
 #pragma unroll 1
     for (int j = 0; j < kCand; ++j) {
@@ -468,12 +476,18 @@ __device__ __forceinline__ void grad_pre_tile(const GradParams& prm, const Src& 
         site_at(id, slot, g, col);
         float v[NV];
         candidate_values<true, NV>(g, col, ux, uy, inv_s2, inv_scale, wt, dLdp, pred, rv, prm.removal_fix_mul, v);
-        if (slot >= 0)
-            sm.vals.add_unique(slot, TileWords<NV>::block_of(slot, rbits), v);
-        else
+        if (slot < 0)
             global_add<true, NV>(prm, id, v);
+        else if (lanes)
+            sm.lanes.add(slot, lane, v, prm.fix12, sm.dkey);
+        else
+            sm.vals.add_unique(slot, TileWords<NV>::block_of(slot, rbits), v);
     }
     __syncthreads();
+    if (lanes) {
+        sm.lanes.flush(used, tid, prm.fix12, sm.dkey);
+        return;
+    }
     for (int d = tid; d < used; d += 256) {
         long long* o = prm.fix12 + static_cast<size_t>(sm.dkey[d]) * 12;
 #pragma unroll
