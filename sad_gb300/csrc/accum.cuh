@@ -273,7 +273,7 @@ struct TileWords {
 // over the same shared memory as TileWords.  The adds of one instruction then land in 32
 // banks, one per lane, and every lane may walk its candidates in the same order, which
 // makes the staged site records' loads broadcasts: in a late-fit ncu capture the L1/shared
-// pipe fell from 77% to 57% of its peak.  A word sums at most 8 terms (one pixel per warp; a
+// pipe fell from 77% to 59% of its peak.  A word sums at most 8 terms (one pixel per warp; a
 // pixel adds to an entry once) of |x| < 2^22, so an entry's 32 lane words sum to less than
 // 2^30; a term of |v| >= 1/4 adds its low part here and its high part straight to the
 // site's global record (an exact integer add, like the flush).
