@@ -283,8 +283,10 @@ def test_trainer_gradients_match_oracle(ops, orc, w, h, n, field, removal, maske
     inputs.  The random fields put far more than a tile table's 256 keys in each 16x16 tile
     (the global path) and repeat ids within lists; the k-nearest fields are what a fit
     sees, and at 6000 sites on 96x80 they too overflow the tables; the sparse k-nearest
-    fields (80-120 pixels per site, the density of the late fit) give every lane of a warp
-    nearly the same list, with masked and partial warps among them.  (A random field that
+    fields (58-102 pixels per site, the density of the late fit) give every lane of a warp
+    nearly the same list, with masked and partial warps among them, and put most of their
+    tiles (28-60 per launch, at most 24 keys each) on the lane-word tables beside tiles on
+    the row copies.  (A random field that
     dense is not used against the oracle: its far candidates give single-pixel terms of
     ~1e-6 whose FP32 value, identical in both GPU kernels, is ill-conditioned.)  Fixed
     point: the same sums to the last bit on a second run."""
