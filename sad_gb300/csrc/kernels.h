@@ -37,7 +37,8 @@ struct BatchArgs {
 
 // Calls launch(args, blocks) for each run of up to kBatchLaunchItems images of the host
 // arrays items[n] and prefix[n + 1] (prefix[i]: image i's first block; prefix[0] = 0),
-// skipping runs without blocks.
+// skipping runs without blocks.  The arguments are built on the caller's stack (at most
+// 22 KB, for the gradient kernel's items).
 template <class Item, class Launch>
 inline void for_each_batch_launch(const Item* items, const uint32_t* prefix, uint32_t n, Launch&& launch) {
     static_assert(sizeof(BatchArgs<Item>) <= 32000, "kernel parameters are limited to 32,764 bytes");
